@@ -1,0 +1,177 @@
+/*
+ * siting.h — C ABI of the GB300 observer-siting library (libsiting_gb300.so).
+ *
+ * The reference (wenlili/siting) is one program per run: the CLI
+ *   cusite nrows roi height targets bw nwanted intervis inputfile outputfile
+ * (siting.cu:746-919, siting.cpp:632-780) calling four C-style stage
+ * functions on raw buffers.  This header replaces that boundary with plain
+ * extern "C" entry points: pointers and sizes only, an int status instead of
+ * exit(1), and a context that owns the CUDA stream and the device workspace.
+ *
+ * Every stage keeps the reference's argument order and meaning.  Two forms
+ * exist for each:
+ *   siting_<stage>(...)      host buffers; copies in, runs, copies out and
+ *                            returns when the results are in host memory
+ *                            (the synchronous behaviour of siting.cu).
+ *   siting_<stage>_dev(...)  device buffers; stream-ordered on the context's
+ *                            stream, returns after enqueueing.
+ * Results are bit-identical to the reference's sequential program (seqsite).
+ *
+ * Status codes: 0 = success; otherwise a SITING_E* value, and
+ * siting_last_error(ctx) returns a message.  Argument checks give the same
+ * messages as the reference's die() calls (siting.cpp:680-695).
+ */
+#ifndef SITING_GB300_H
+#define SITING_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define SITING_OK 0
+#define SITING_EINVAL 1   /* argument outside the accepted range */
+#define SITING_ENOMEM 2   /* device allocation failed or HBM budget exceeded */
+#define SITING_ECUDA 3    /* CUDA runtime error */
+#define SITING_ETIMEOUT 4 /* a bounded device wait expired (no fault) */
+#define SITING_EIO 5      /* file input/output */
+#define SITING_EDEVICE 6  /* no usable device / unsupported architecture */
+
+typedef struct siting_ctx siting_ctx;
+
+/* One siting job: the nine CLI arguments minus the two file names
+ * (siting.cpp:668-674; oht = tht = height there). */
+typedef struct siting_params {
+  int nrows;    /* DEM side, cells */
+  int roi;      /* radius of interest, cells */
+  int oht;      /* observer height above ground */
+  int tht;      /* target height above ground */
+  int ntests;   /* random targets per cell ("targets") */
+  int bw;       /* requested block width ("bw", blocksize0) */
+  int nwanted0; /* requested tentative observers ("nwanted") */
+  int intervis; /* 1: new observers must be visible from earlier ones */
+} siting_params;
+
+/* Perturbed block geometry of siting.cpp:688-695. */
+typedef struct siting_geometry {
+  float blocksize;
+  int nblocks;
+  int nwantedperblock;
+  int nwanted;
+} siting_geometry;
+
+/* Outcome and per-stage device times of one job. */
+typedef struct siting_result {
+  int nusedsheds;    /* observers selected (siting.cpp:617) */
+  long long cumarea; /* cells covered by the selected viewsheds */
+  double coverage;   /* 100.0 * cumarea / nrows^2, as printed by siting.cpp:617 */
+  int nwanted;       /* tentative observers after the geometry perturbation */
+  float ms_vix, ms_findmax, ms_viewshed, ms_site; /* CUDA-event stage times */
+  float ms_h2d, ms_d2h;                           /* copies (host forms) */
+  int site_rounds;   /* greedy rounds run on the device */
+} siting_result;
+
+/* ---- errors ----------------------------------------------------------- */
+const char *siting_status_string(int status);
+/* Message of the last failing call on ctx (never NULL). */
+const char *siting_last_error(const siting_ctx *ctx);
+
+/* ---- validation and geometry (no device needed) ------------------------ */
+/* Range checks of siting.cpp:680-686 plus the last-block check of
+ * siting.cpp:693-695; writes the reference's message to msg on failure.
+ * lib_form != 0 accepts the library-only relaxations (bw >= 1, nwanted0 >= 1)
+ * used by the batched and serving workloads. */
+int siting_validate(const siting_params *p, int lib_form, char *msg,
+                    size_t msg_cap);
+/* Block geometry of siting.cpp:688-695. */
+int siting_block_geometry(int nrows, int bw, int nwanted0,
+                          siting_geometry *out);
+
+/* ---- context ------------------------------------------------------------ */
+/* Creates a context on `device` with its own non-blocking stream.  hbm_budget
+ * caps the workspace bytes the context may hold (0 = no cap). */
+int siting_ctx_create(int device, size_t hbm_budget, siting_ctx **out);
+int siting_ctx_destroy(siting_ctx *ctx);
+/* Waits for all work enqueued on the context's stream. */
+int siting_ctx_sync(siting_ctx *ctx);
+/* The context's cudaStream_t, as an opaque pointer. */
+void *siting_ctx_stream(siting_ctx *ctx);
+/* Workspace bytes currently held. */
+size_t siting_ctx_workspace_bytes(const siting_ctx *ctx);
+/* Releases the workspace (buffers are re-created on demand). */
+int siting_ctx_trim(siting_ctx *ctx);
+/* Tuning knob: CTAs of the SITE kernel (0 = automatic, capped at the SM
+ * count).  Results do not depend on it. */
+int siting_ctx_set_site_ctas(siting_ctx *ctx, int nctas);
+/* Page-locked host memory for fast copies (cudaMallocHost / cudaFreeHost). */
+int siting_pinned_alloc(size_t bytes, void **out);
+int siting_pinned_free(void *p);
+
+/* ---- stage 1: VIX (replaces calc_vix, siting.cpp:192 / siting.cu:133) --- */
+int siting_calc_vix(siting_ctx *ctx, int nrows, const uint16_t *elevs,
+                    int roi, int oht, int tht, int ntests, uint8_t *vix);
+int siting_calc_vix_dev(siting_ctx *ctx, int nrows, const uint16_t *d_elevs,
+                        int roi, int oht, int tht, int ntests, uint8_t *d_vix);
+
+/* ---- stage 2: FINDMAX (replaces find_max, siting.cpp:235 / siting.cu:226).
+ * vix is modified as in siting.cpp: each winner's entry is cleared. -------- */
+int siting_find_max(siting_ctx *ctx, int nrows, uint8_t *vix, float blocksize,
+                    int nwanted, int nblocks, int nwantedperblock,
+                    int32_t *obs);
+int siting_find_max_dev(siting_ctx *ctx, int nrows, uint8_t *d_vix,
+                        float blocksize, int nwanted, int nblocks,
+                        int nwantedperblock, int32_t *d_obs);
+
+/* ---- stage 3: VIEWSHED (replaces calc_sheds, siting.cpp:349 /
+ * siting.cu:336).  sheds: nsheds * (2roi+1) * ceil((2roi+1)/64) words,
+ * bit (r,c) at word r*nwpr + c/64, bit 63 - c%64 (siting.cpp:247-250). ----- */
+int siting_calc_sheds(siting_ctx *ctx, int nrows, const uint16_t *elevs,
+                      int roi, int oht, int tht, int nsheds,
+                      const int32_t *obs, uint64_t *sheds);
+int siting_calc_sheds_dev(siting_ctx *ctx, int nrows, const uint16_t *d_elevs,
+                          int roi, int oht, int tht, int nsheds,
+                          const int32_t *d_obs, uint64_t *d_sheds);
+
+/* ---- stage 4: SITE (replaces site_it, siting.cpp:501 / siting.cu:596).
+ * selected[i] = 1 for chosen observers.  res may be NULL. ---------------- */
+int siting_site_it(siting_ctx *ctx, int nrows, int roi, int intervis,
+                   int nsheds, const int32_t *obs, const uint64_t *sheds,
+                   uint8_t *selected, siting_result *res);
+int siting_site_it_dev(siting_ctx *ctx, int nrows, int roi, int intervis,
+                       int nsheds, const int32_t *d_obs,
+                       const uint64_t *d_sheds, uint8_t *d_selected,
+                       siting_result *res);
+
+/* ---- whole pipeline (replaces main's stage sequence, siting.cpp:737-759).
+ * obs and selected receive nwanted entries (see siting_block_geometry). --- */
+int siting_run(siting_ctx *ctx, const siting_params *p, const uint16_t *elevs,
+               int32_t *obs, uint8_t *selected, siting_result *res);
+/* Device-resident form: d_elevs is nrows*nrows uint16 on the device; obs and
+ * selected (device) receive nwanted entries.  Intermediate VIX and viewshed
+ * arrays stay in the context's workspace. */
+int siting_run_dev(siting_ctx *ctx, const siting_params *p,
+                   const uint16_t *d_elevs, int32_t *d_obs,
+                   uint8_t *d_selected, siting_result *res);
+
+/* ---- files (the reference's input and output formats) ------------------ */
+/* Reads exactly nrows*nrows uint16 (siting.cpp:726-730). */
+int siting_read_dem(const char *path, int nrows, uint16_t *out);
+/* Writes "x,y\n" per selected observer in index order (siting.cpp:761-765). */
+int siting_write_observers(const char *path, int nrows, int nsheds,
+                           const int32_t *obs, const uint8_t *selected);
+
+/* ---- synthetic terrain ------------------------------------------------- */
+/* Seeded fBm value noise (optionally blended with ridged noise), min-max
+ * scaled to [0, range_max], row-major uint16.  Host only; deterministic
+ * across hosts. */
+int siting_fbm_dem(uint16_t *out, int nrows, uint64_t seed, int octaves,
+                   double persistence, double lacunarity,
+                   double base_wavelength, double ridged_weight,
+                   int range_max);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* SITING_GB300_H */

@@ -1,0 +1,354 @@
+"""GB300 observer siting: VIX -> FINDMAX -> VIEWSHED -> SITE.
+
+Python mirror of the library's C ABI (include/siting.h).  The stage functions
+keep the reference's names, argument order and meaning (wenlili/siting:
+calc_vix siting.cpp:192, find_max siting.cpp:235, calc_sheds siting.cpp:349,
+site_it siting.cpp:501); errors raise ``SitingError`` carrying the library's
+status and message instead of the reference's exit(1).
+
+All compute runs in the CUDA kernels of ``libsiting_gb300.so``.  There is no
+CPU fallback: importing works without the library (for building), but every
+call that needs it raises if it is missing.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+from dataclasses import dataclass
+
+import numpy as np
+
+__all__ = [
+    "SitingError", "Params", "Geometry", "Result", "Context", "load", "block_geometry",
+    "validate", "fbm_dem", "read_dem", "write_observers", "observers_text", "LIB_PATH",
+    "CLI_PATH", "shed_words",
+]
+
+_PKG = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_PKG, "libsiting_gb300.so")
+CLI_PATH = os.path.join(_PKG, "cusite")
+
+OK, EINVAL, ENOMEM, ECUDA, ETIMEOUT, EIO, EDEVICE = range(7)
+
+
+class SitingError(RuntimeError):
+    def __init__(self, status: int, message: str):
+        super().__init__(f"[{status}] {message}")
+        self.status = status
+        self.message = message
+
+
+class _ParamsC(C.Structure):
+    _fields_ = [("nrows", C.c_int), ("roi", C.c_int), ("oht", C.c_int), ("tht", C.c_int),
+                ("ntests", C.c_int), ("bw", C.c_int), ("nwanted0", C.c_int),
+                ("intervis", C.c_int)]
+
+
+class _GeometryC(C.Structure):
+    _fields_ = [("blocksize", C.c_float), ("nblocks", C.c_int), ("nwantedperblock", C.c_int),
+                ("nwanted", C.c_int)]
+
+
+class _ResultC(C.Structure):
+    _fields_ = [("nusedsheds", C.c_int), ("cumarea", C.c_longlong), ("coverage", C.c_double),
+                ("nwanted", C.c_int), ("ms_vix", C.c_float), ("ms_findmax", C.c_float),
+                ("ms_viewshed", C.c_float), ("ms_site", C.c_float), ("ms_h2d", C.c_float),
+                ("ms_d2h", C.c_float), ("site_rounds", C.c_int)]
+
+
+@dataclass
+class Params:
+    """One job: the CLI's nine arguments minus the file names."""
+    nrows: int
+    roi: int
+    height: int = 0
+    ntests: int = 50
+    bw: int = 10
+    nwanted0: int = 10000
+    intervis: int = 0
+    oht: int | None = None
+    tht: int | None = None
+
+    def c(self) -> _ParamsC:
+        oht = self.height if self.oht is None else self.oht
+        tht = self.height if self.tht is None else self.tht
+        return _ParamsC(self.nrows, self.roi, oht, tht, self.ntests, self.bw, self.nwanted0,
+                        self.intervis)
+
+
+@dataclass
+class Geometry:
+    blocksize: float
+    nblocks: int
+    nwantedperblock: int
+    nwanted: int
+
+
+@dataclass
+class Result:
+    nusedsheds: int
+    cumarea: int
+    coverage: float
+    nwanted: int
+    ms_vix: float
+    ms_findmax: float
+    ms_viewshed: float
+    ms_site: float
+    ms_h2d: float
+    ms_d2h: float
+    site_rounds: int
+
+    @staticmethod
+    def of(r: _ResultC) -> "Result":
+        return Result(*(getattr(r, f) for f, _ in _ResultC._fields_))
+
+
+_lib = None
+_P = C.c_void_p
+
+
+def load() -> C.CDLL:
+    """Loads libsiting_gb300.so (raises if it has not been built)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        raise SitingError(EDEVICE, f"{LIB_PATH} is missing: run siting_gb300.build.build() first")
+    lib = C.CDLL(LIB_PATH)
+    i, f, ll, sz = C.c_int, C.c_float, C.c_longlong, C.c_size_t
+    sig = {
+        "siting_status_string": ([i], C.c_char_p),
+        "siting_last_error": ([_P], C.c_char_p),
+        "siting_validate": ([C.POINTER(_ParamsC), i, C.c_char_p, sz], i),
+        "siting_block_geometry": ([i, i, i, C.POINTER(_GeometryC)], i),
+        "siting_ctx_create": ([i, sz, C.POINTER(_P)], i),
+        "siting_ctx_destroy": ([_P], i),
+        "siting_ctx_sync": ([_P], i),
+        "siting_ctx_stream": ([_P], _P),
+        "siting_ctx_workspace_bytes": ([_P], sz),
+        "siting_ctx_trim": ([_P], i),
+        "siting_ctx_set_site_ctas": ([_P, i], i),
+        "siting_pinned_alloc": ([sz, C.POINTER(_P)], i),
+        "siting_pinned_free": ([_P], i),
+        "siting_calc_vix": ([_P, i, _P, i, i, i, i, _P], i),
+        "siting_calc_vix_dev": ([_P, i, _P, i, i, i, i, _P], i),
+        "siting_find_max": ([_P, i, _P, f, i, i, i, _P], i),
+        "siting_find_max_dev": ([_P, i, _P, f, i, i, i, _P], i),
+        "siting_calc_sheds": ([_P, i, _P, i, i, i, i, _P, _P], i),
+        "siting_calc_sheds_dev": ([_P, i, _P, i, i, i, i, _P, _P], i),
+        "siting_site_it": ([_P, i, i, i, i, _P, _P, _P, C.POINTER(_ResultC)], i),
+        "siting_site_it_dev": ([_P, i, i, i, i, _P, _P, _P, C.POINTER(_ResultC)], i),
+        "siting_run": ([_P, C.POINTER(_ParamsC), _P, _P, _P, C.POINTER(_ResultC)], i),
+        "siting_run_dev": ([_P, C.POINTER(_ParamsC), _P, _P, _P, C.POINTER(_ResultC)], i),
+        "siting_read_dem": ([C.c_char_p, i, _P], i),
+        "siting_write_observers": ([C.c_char_p, i, i, _P, _P], i),
+        "siting_fbm_dem": ([_P, i, C.c_uint64, i, C.c_double, C.c_double, C.c_double,
+                            C.c_double, i], i),
+    }
+    for name, (argt, rest) in sig.items():
+        fn = getattr(lib, name)
+        fn.argtypes = argt
+        fn.restype = rest
+    _lib = lib
+    return lib
+
+
+def shed_words(roi: int) -> int:
+    """uint64 words per viewshed: (2roi+1) * ceil((2roi+1)/64)."""
+    nr = 2 * roi + 1
+    return nr * ((nr + 63) // 64)
+
+
+def _ptr(a) -> int:
+    if a is None:
+        return None
+    if hasattr(a, "data_ptr"):
+        return a.data_ptr()
+    if isinstance(a, np.ndarray):
+        return a.ctypes.data
+    return int(a)
+
+
+def block_geometry(nrows: int, bw: int, nwanted0: int) -> Geometry:
+    g = _GeometryC()
+    rc = load().siting_block_geometry(nrows, bw, nwanted0, C.byref(g))
+    if rc:
+        raise SitingError(rc, "The last block is too small for nwantedperblock.")
+    return Geometry(g.blocksize, g.nblocks, g.nwantedperblock, g.nwanted)
+
+
+def validate(p: Params, lib_form: bool = True) -> str | None:
+    """Returns None if p is acceptable, else the reference's message."""
+    buf = C.create_string_buffer(256)
+    pc = p.c()
+    rc = load().siting_validate(C.byref(pc), 1 if lib_form else 0, buf, 256)
+    return None if rc == OK else buf.value.decode()
+
+
+def fbm_dem(nrows: int, seed: int, octaves: int = 8, persistence: float = 0.5,
+            lacunarity: float = 2.0, base_wavelength: float = 256.0, ridged_weight: float = 0.0,
+            range_max: int = 10000) -> np.ndarray:
+    """Seeded fBm terrain, uint16[nrows*nrows] row-major."""
+    out = np.empty(nrows * nrows, np.uint16)
+    rc = load().siting_fbm_dem(out.ctypes.data, nrows, seed, octaves, persistence, lacunarity,
+                               base_wavelength, ridged_weight, range_max)
+    if rc:
+        raise SitingError(rc, "fbm_dem: invalid arguments")
+    return out
+
+
+def read_dem(path: str, nrows: int) -> np.ndarray:
+    out = np.empty(nrows * nrows, np.uint16)
+    rc = load().siting_read_dem(path.encode(), nrows, out.ctypes.data)
+    if rc:
+        raise SitingError(rc, "Input failed")
+    return out
+
+
+def write_observers(path: str, nrows: int, obs: np.ndarray, selected: np.ndarray) -> None:
+    obs = np.ascontiguousarray(obs, np.int32)
+    selected = np.ascontiguousarray(selected, np.uint8)
+    rc = load().siting_write_observers(path.encode(), nrows, len(obs), obs.ctypes.data,
+                                       selected.ctypes.data)
+    if rc:
+        raise SitingError(rc, "Output failed")
+
+
+def observers_text(obs: np.ndarray, selected: np.ndarray, nrows: int) -> bytes:
+    """The observers file's bytes: 'x,y\\n' per selected index in index order."""
+    idx = np.nonzero(np.asarray(selected))[0]
+    o = np.asarray(obs)[idx]
+    return "".join(f"{v // nrows},{v % nrows}\n" for v in o.tolist()).encode()
+
+
+class Context:
+    """A device context: CUDA stream + resident workspace (HBM budget)."""
+
+    def __init__(self, device: int = 0, hbm_budget: int = 0):
+        self._lib = load()
+        h = _P()
+        rc = self._lib.siting_ctx_create(device, hbm_budget, C.byref(h))
+        if rc:
+            raise SitingError(rc, f"siting_ctx_create(device={device}) failed: "
+                                  f"{self._lib.siting_status_string(rc).decode()}")
+        self.h = h
+
+    def close(self):
+        if getattr(self, "h", None):
+            self._lib.siting_ctx_destroy(self.h)
+            self.h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _check(self, rc: int):
+        if rc:
+            raise SitingError(rc, self._lib.siting_last_error(self.h).decode())
+
+    @property
+    def stream(self) -> int:
+        return self._lib.siting_ctx_stream(self.h) or 0
+
+    def sync(self):
+        self._check(self._lib.siting_ctx_sync(self.h))
+
+    def workspace_bytes(self) -> int:
+        return self._lib.siting_ctx_workspace_bytes(self.h)
+
+    def trim(self):
+        self._check(self._lib.siting_ctx_trim(self.h))
+
+    def set_site_ctas(self, n: int):
+        self._check(self._lib.siting_ctx_set_site_ctas(self.h, n))
+
+    # ---- stages on host arrays (reference signatures) -----------------------
+    def calc_vix(self, nrows, elevs, roi, oht, tht, ntests) -> np.ndarray:
+        elevs = np.ascontiguousarray(elevs, np.uint16).ravel()
+        vix = np.empty(nrows * nrows, np.uint8)
+        self._check(self._lib.siting_calc_vix(self.h, nrows, elevs.ctypes.data, roi, oht, tht,
+                                              ntests, vix.ctypes.data))
+        return vix
+
+    def find_max(self, nrows, vix, blocksize, nwanted, nblocks, nwantedperblock) -> np.ndarray:
+        """Returns obs; `vix` (uint8 numpy, modified in place as the reference does)."""
+        assert vix.dtype == np.uint8 and vix.flags.c_contiguous
+        obs = np.empty(nwanted, np.int32)
+        self._check(self._lib.siting_find_max(self.h, nrows, vix.ctypes.data, blocksize, nwanted,
+                                              nblocks, nwantedperblock, obs.ctypes.data))
+        return obs
+
+    def calc_sheds(self, nrows, elevs, roi, oht, tht, obs) -> np.ndarray:
+        elevs = np.ascontiguousarray(elevs, np.uint16).ravel()
+        obs = np.ascontiguousarray(obs, np.int32)
+        sheds = np.empty(len(obs) * shed_words(roi), np.uint64)
+        self._check(self._lib.siting_calc_sheds(self.h, nrows, elevs.ctypes.data, roi, oht, tht,
+                                                len(obs), obs.ctypes.data, sheds.ctypes.data))
+        return sheds
+
+    def site_it(self, nrows, roi, intervis, obs, sheds):
+        """Returns (selected uint8[nsheds], Result)."""
+        obs = np.ascontiguousarray(obs, np.int32)
+        sheds = np.ascontiguousarray(sheds, np.uint64)
+        sel = np.empty(len(obs), np.uint8)
+        r = _ResultC()
+        self._check(self._lib.siting_site_it(self.h, nrows, roi, intervis, len(obs),
+                                             obs.ctypes.data, sheds.ctypes.data, sel.ctypes.data,
+                                             C.byref(r)))
+        return sel, Result.of(r)
+
+    # ---- stages on device buffers (pointers or torch tensors) ----------------
+    def calc_vix_dev(self, nrows, d_elevs, roi, oht, tht, ntests, d_vix):
+        self._check(self._lib.siting_calc_vix_dev(self.h, nrows, _ptr(d_elevs), roi, oht, tht,
+                                                  ntests, _ptr(d_vix)))
+
+    def find_max_dev(self, nrows, d_vix, blocksize, nwanted, nblocks, npb, d_obs):
+        self._check(self._lib.siting_find_max_dev(self.h, nrows, _ptr(d_vix), blocksize, nwanted,
+                                                  nblocks, npb, _ptr(d_obs)))
+
+    def calc_sheds_dev(self, nrows, d_elevs, roi, oht, tht, nsheds, d_obs, d_sheds):
+        self._check(self._lib.siting_calc_sheds_dev(self.h, nrows, _ptr(d_elevs), roi, oht, tht,
+                                                    nsheds, _ptr(d_obs), _ptr(d_sheds)))
+
+    def site_it_dev(self, nrows, roi, intervis, nsheds, d_obs, d_sheds, d_selected) -> Result:
+        r = _ResultC()
+        self._check(self._lib.siting_site_it_dev(self.h, nrows, roi, intervis, nsheds, _ptr(d_obs),
+                                                 _ptr(d_sheds), _ptr(d_selected), C.byref(r)))
+        return Result.of(r)
+
+    # ---- whole pipeline ---------------------------------------------------------
+    def run(self, p: Params, elevs):
+        """Host DEM in, (obs, selected, Result) out."""
+        elevs = np.ascontiguousarray(elevs, np.uint16).ravel() if isinstance(elevs, np.ndarray) \
+            else elevs
+        g = block_geometry(p.nrows, p.bw, p.nwanted0)
+        obs = np.empty(g.nwanted, np.int32)
+        sel = np.empty(g.nwanted, np.uint8)
+        r = _ResultC()
+        pc = p.c()
+        self._check(self._lib.siting_run(self.h, C.byref(pc), _ptr(elevs), obs.ctypes.data,
+                                         sel.ctypes.data, C.byref(r)))
+        return obs, sel, Result.of(r)
+
+    def run_into(self, p: Params, elevs_ptr, obs_ptr, sel_ptr) -> Result:
+        """Host pointers (e.g. pinned buffers) in and out."""
+        r = _ResultC()
+        pc = p.c()
+        self._check(self._lib.siting_run(self.h, C.byref(pc), _ptr(elevs_ptr), _ptr(obs_ptr),
+                                         _ptr(sel_ptr), C.byref(r)))
+        return Result.of(r)
+
+    def run_dev(self, p: Params, d_elevs, d_obs, d_selected) -> Result:
+        r = _ResultC()
+        pc = p.c()
+        self._check(self._lib.siting_run_dev(self.h, C.byref(pc), _ptr(d_elevs), _ptr(d_obs),
+                                             _ptr(d_selected), C.byref(r)))
+        return Result.of(r)

@@ -1,0 +1,131 @@
+// Device helpers shared by the siting kernels (sm_103a).
+#pragma once
+
+#include <cuda.h>
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "kernels.h"
+
+namespace siting {
+
+// Bounded waits: ~2^31 cycles (about a second at GB300 clocks).
+constexpr long long kWaitCycles = 1ll << 31;
+
+// ---- reference arithmetic --------------------------------------------------
+// glibc LCG step on 31 bits (siting.cpp:29-33).
+__host__ __device__ __forceinline__ uint32_t lcg_step(uint32_t s) {
+  return (1103515245u * (s & 0x7fffffffu) + 12345u) & 0x7fffffffu;
+}
+
+// FP32 operations with explicit round-to-nearest so that nvcc never contracts
+// a multiply and an add into an FMA (the reference's results are those of
+// separately rounded operations).
+__device__ __forceinline__ float fmul(float a, float b) { return __fmul_rn(a, b); }
+__device__ __forceinline__ float fadd(float a, float b) { return __fadd_rn(a, b); }
+__device__ __forceinline__ float fdiv(float a, float b) { return __fdiv_rn(a, b); }
+__device__ __forceinline__ float i2f(int v) { return __int2float_rn(v); }
+__device__ __forceinline__ int f2i(float v) { return __float2int_rz(v); }
+// (int)round(v): half away from zero, as C's round()/roundf().
+__device__ __forceinline__ int round_i(float v) { return __float2int_rz(roundf(v)); }
+
+// ---- memory-order helpers --------------------------------------------------
+__device__ __forceinline__ unsigned ld_acquire_u32(const unsigned *p) {
+  unsigned v;
+  asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+__device__ __forceinline__ void st_release_u32(unsigned *p, unsigned v) {
+  asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+
+// ---- mbarrier + TMA (cp.async.bulk.tensor) ---------------------------------
+__device__ __forceinline__ uint32_t smem_u32(const void *p) {
+  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+
+__device__ __forceinline__ void mbar_init(uint64_t *bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count)
+               : "memory");
+  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+
+__device__ __forceinline__ void mbar_expect_tx(uint64_t *bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)),
+               "r"(bytes)
+               : "memory");
+}
+
+// Waits for phase `parity` of the mbarrier; false if the bounded wait expired.
+__device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity) {
+  const uint32_t addr = smem_u32(bar);
+  const long long t0 = clock64();
+  for (;;) {
+    uint32_t done;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(done)
+        : "r"(addr), "r"(parity)
+        : "memory");
+    if (done) return true;
+    if (clock64() - t0 > kWaitCycles) return false;
+  }
+}
+
+// 2-D tiled TMA load of box {c0 (inner, elements), r0 (outer)} into smem.
+__device__ __forceinline__ void tma_load_2d(void *dst, const CUtensorMap *map, int c0, int r0,
+                                            uint64_t *bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes"
+      " [%0], [%1, {%2, %3}], [%4];" ::"r"(smem_u32(dst)),
+      "l"(reinterpret_cast<uint64_t>(map)), "r"(c0), "r"(r0), "r"(smem_u32(bar))
+      : "memory");
+}
+
+// ---- bounded barrier over a group of co-resident CTAs ------------------------
+// bar[0] = arrival count, bar[1] = generation.  Must be reached by all
+// threads of every CTA of the group.  Returns false (and sets err) when the
+// wait expired; the group then abandons its work.
+struct GroupBarrier {
+  unsigned *bar;
+  unsigned nctas;
+  unsigned gen;
+};
+
+__device__ __forceinline__ bool group_sync(GroupBarrier &b, int *err, int *s_flag) {
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    int ok = 1;
+    __threadfence();
+    const unsigned g = b.gen;
+    const unsigned arrived = atomicAdd(&b.bar[0], 1u);
+    if (arrived == b.nctas - 1) {
+      atomicExch(&b.bar[0], 0u);
+      __threadfence();
+      st_release_u32(&b.bar[1], g + 1);
+    } else {
+      const long long t0 = clock64();
+      while (ld_acquire_u32(&b.bar[1]) == g) {
+        if (clock64() - t0 > kWaitCycles) {
+          atomicOr(err, kErrBarrierTimeout);
+          ok = 0;
+          break;
+        }
+      }
+    }
+    b.gen = g + 1;
+    __threadfence();
+    *s_flag = ok;
+  }
+  __syncthreads();
+  const bool ok = *s_flag != 0;
+  __syncthreads();
+  return ok;
+}
+
+__host__ __device__ __forceinline__ int ceil_div(int a, int b) { return (a + b - 1) / b; }
+
+}  // namespace siting

@@ -1,0 +1,88 @@
+// Host-side launch interface of the four stage kernels (internal to the
+// library; the public boundary is include/siting.h).
+#pragma once
+
+#include <cuda.h>
+#include <cuda_runtime.h>
+#include <stddef.h>
+#include <stdint.h>
+
+namespace siting {
+
+// ---- error flags written by kernels (never a trap or a fault) -------------
+enum : int {
+  kErrTmaTimeout = 1,      // an mbarrier wait for a TMA tile expired
+  kErrBarrierTimeout = 2,  // a grid-group barrier wait expired
+  kErrSiteMismatch = 4,    // SITE self-check: pick gain != its new coverage
+  kErrCapacity = 8,        // a per-CTA work list overflowed its capacity
+  kErrBadInput = 16,       // an observer index outside the DEM
+};
+
+
+// A DEM resident on the device: row-major uint16, `pitch` elements per row.
+struct DemView {
+  const uint16_t *data;
+  int nrows;
+  int pitch;
+  bool tma_ok;  // pitch*2 % 16 == 0 and data 16-byte aligned
+};
+
+// Encodes a 2-D TMA descriptor over a DEM with box {box_w, box_h}.
+bool make_dem_tensor_map(CUtensorMap *map, const DemView &dem, int box_w, int box_h);
+
+// ---- VIX -------------------------------------------------------------------
+struct VixPlan {
+  int tile;       // cells per tile side
+  int threads;    // threads per CTA
+  bool use_smem;  // stage the halo tile in shared memory by TMA
+};
+// Device tables of the VIX stage (host-computed with the reference's
+// expressions): jump[2k], jump[2k+1] = LCG multiplier/increment of k+1 steps
+// for k < 2*ntests; rtab[d] = (float)(1.0/d); vtab[v] = VIX byte of v hits.
+size_t vix_table_bytes(int roi, int ntests);
+void vix_fill_tables(void *host_buf, int roi, int ntests);
+VixPlan vix_default_plan(int nrows, int roi, int ntests);
+size_t vix_smem_bytes(const VixPlan &p, int roi, int ntests);
+cudaError_t launch_vix(const DemView &dem, int roi, int oht, int tht, int ntests,
+                       uint8_t *vix, const void *d_tables, const VixPlan &plan, int *d_err,
+                       cudaStream_t st);
+
+// ---- FINDMAX -----------------------------------------------------------------
+cudaError_t launch_findmax(uint8_t *vix, int nrows, float blocksize, int nblocks, int npb,
+                           int32_t *obs, cudaStream_t st);
+
+// Sets kErrBadInput in *d_err if any obs[i] is outside [0, nrows^2).
+cudaError_t launch_check_obs(const int32_t *obs, int nsheds, int nrows, int *d_err,
+                             cudaStream_t st);
+
+// ---- VIEWSHED -----------------------------------------------------------------
+struct ShedPlan {
+  int threads;
+  bool use_smem;  // stage the (2roi+1)^2 window by TMA
+};
+ShedPlan shed_default_plan(int roi);
+size_t shed_smem_bytes(const ShedPlan &p, int roi);
+cudaError_t launch_sheds(const DemView &dem, int roi, int oht, int tht, int nsheds,
+                         const int32_t *obs, uint64_t *sheds, const ShedPlan &plan, int *d_err,
+                         cudaStream_t st);
+
+// ---- SITE -----------------------------------------------------------------------
+// Scratch layout of one SITE job (device, carved from one allocation).
+struct SiteScratch {
+  uint64_t *cum[2];   // nrows * ceil(nrows/64) words each, zeroed before launch
+  uint64_t *slots;    // 2 * nctas * 2 words: {key, pos} per CTA per parity
+  unsigned *bar;      // 2 words, zeroed
+  long long *out;     // [0] nused, [1] cumarea, [2] rounds
+  int32_t *order;     // nsheds: picks in order
+};
+size_t site_scratch_bytes(int nrows, int nsheds, int nctas);
+void site_carve_scratch(void *base, int nrows, int nsheds, int nctas, SiteScratch *s);
+int site_default_ctas(int nsheds, int sm_count);
+size_t site_smem_bytes(int roi, int nsheds, int nctas, int nblocks, int npb, float blocksize);
+bool site_supported(int roi, int nsheds, int nctas);
+cudaError_t launch_site(int nrows, int roi, int intervis, int nsheds, const int32_t *obs,
+                        const uint64_t *sheds, float blocksize, int nblocks, int npb,
+                        uint8_t *selected, const SiteScratch &s, int nctas, int *d_err,
+                        cudaStream_t st);
+
+}  // namespace siting

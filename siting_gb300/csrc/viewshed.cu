@@ -1,0 +1,223 @@
+// VIEWSHED: bit-packed viewshed of every tentative observer
+// (siting.cpp:247-360).
+//
+// From observer o, rays go to each of the 8*roi perimeter cells of the
+// (2roi+1)^2 box (perimeter order of siting.cpp:291-304).  A ray steps the
+// major axis, puts the minor coordinate at o + round(i*slope), stops at the
+// DEM edge or outside the roi circle, keeps the running maximum horizon slope
+// s = (elev - oalt)/|i| and marks the cell when elev + tht >= oalt + hs*|i|.
+// Bit (row, col) of a shed is word row*nwpr + col/64, bit 63 - col%64.
+//
+// GB300 mapping: one CTA per observer.  The observer's window (2roi+1 rows,
+// 2roi+8 columns from an 8-aligned start) is loaded into shared memory by one
+// TMA bulk-tensor copy; each thread sweeps rays (adjacent threads take
+// adjacent perimeter cells, so a warp's lanes touch neighbouring cells each
+// step and have nearly equal ray lengths).  Visible cells are OR-ed into a
+// shared-memory image of the shed (32-bit halves of the reference's 64-bit
+// words), which is then written to HBM with coalesced stores.  For windows
+// wider than one TMA box the DEM is read through the read-only L1 path.
+//
+// Bit-exactness: separately rounded FP32 operations, IEEE division for the
+// slopes, round-half-away-from-zero for the minor coordinate.
+#include "common.cuh"
+#include "kernels.h"
+
+namespace siting {
+namespace {
+
+struct ShedArgs {
+  const uint16_t *dem;
+  int pitch, n, roi, oht, tht, nsheds;
+  const int32_t *obs;
+  uint64_t *sheds;
+  int win_w, box_rows, nboxes;
+  int *err;
+};
+
+struct SmemDem {
+  const uint16_t *s;
+  int w, x0, y0;
+  __device__ __forceinline__ int at(int x, int y) const { return s[(x - x0) * w + (y - y0)]; }
+};
+
+struct GlobalDem {
+  const uint16_t *g;
+  int pitch;
+  __device__ __forceinline__ int at(int x, int y) const { return __ldg(g + x * pitch + y); }
+};
+
+// Sets bit (row, col) of the shed image held as 32-bit halves of 64-bit words.
+__device__ __forceinline__ void shed_set(unsigned *bits, int nwpr, int row, int col) {
+  const int w = row * nwpr + (col >> 6);
+  const int b = 63 - (col & 63);
+  atomicOr(&bits[2 * w + (b >> 5)], 1u << (b & 31));
+}
+
+template <class Dem>
+__device__ __forceinline__ void sweep_rays(const Dem &dem, const ShedArgs &a, int ox, int oy,
+                                           unsigned *bits) {
+  const int roi = a.roi, n = a.n, side = 2 * roi;
+  const int nwpr = (2 * roi + 1 + 63) / 64;
+  const int roi2 = roi * roi;
+  const int xmin = ox - roi, ymin = oy - roi, xmax = ox + roi, ymax = oy + roi;
+  const int oalt = dem.at(ox, oy) + a.oht;
+  const float foalt = i2f(oalt);
+  for (int ip = threadIdx.x; ip < 4 * side; ip += blockDim.x) {
+    int tx, ty;
+    if (ip < side) {
+      tx = xmin + ip;
+      ty = ymin;
+    } else if (ip < 2 * side) {
+      tx = 1 + xmin - side + ip;
+      ty = ymax;
+    } else if (ip < 3 * side) {
+      tx = xmin;
+      ty = 1 + ymin - 2 * side + ip;
+    } else {
+      tx = xmax;
+      ty = ymin - 3 * side + ip;
+    }
+    if (tx == ox && ty == oy) continue;
+    const int dx = tx - ox, dy = ty - oy;
+    const bool my = abs(dx) < abs(dy);
+    const int dmaj = my ? dy : dx, dmin = my ? dx : dy;
+    const float slope = fdiv(i2f(dmin), i2f(dmaj));
+    const int dir = dmaj > 0 ? 1 : -1;
+    float hs = -99999.f;
+    for (int i = dir; i != dmaj + dir; i += dir) {
+      const int off = round_i(fmul(i2f(i), slope));
+      const int px = my ? ox + off : ox + i;
+      const int py = my ? oy + i : oy + off;
+      if ((unsigned)px >= (unsigned)n || (unsigned)py >= (unsigned)n) break;
+      const int ex = px - ox, ey = py - oy;
+      if (ex * ex + ey * ey > roi2) break;
+      const int pelev = dem.at(px, py);
+      const float fai = i2f(abs(i));
+      const float s = fdiv(i2f(pelev - oalt), fai);
+      if (hs < s) hs = s;
+      const float halt = fadd(foalt, fmul(hs, fai));
+      if (i2f(pelev + a.tht) >= halt) shed_set(bits, nwpr, ex + roi, ey + roi);
+    }
+  }
+}
+
+template <bool kSmem>
+__global__ void __launch_bounds__(256) shed_kernel(const __grid_constant__ CUtensorMap map,
+                                                   const ShedArgs a) {
+  extern __shared__ __align__(128) unsigned char sm[];
+  const int nr = 2 * a.roi + 1, nwpr = (nr + 63) / 64, nwords = nr * nwpr;
+  const int ob = a.obs[blockIdx.x];
+  if (ob < 0 || ob >= a.n * a.n) {  // invalid observer: empty shed, flagged
+    uint64_t *dst = a.sheds + (size_t)blockIdx.x * nwords;
+    for (int i = threadIdx.x; i < nwords; i += blockDim.x) dst[i] = 0ull;
+    if (threadIdx.x == 0) atomicOr(a.err, kErrBadInput);
+    return;
+  }
+  const int ox = ob / a.n, oy = ob - (ob / a.n) * a.n;
+  const int hx0 = ox - a.roi, hy0 = (oy - a.roi) & ~7;
+  uint16_t *win = reinterpret_cast<uint16_t *>(sm);
+  const uint32_t win_bytes = kSmem ? (uint32_t)a.nboxes * a.box_rows * a.win_w * 2u : 0u;
+  uint64_t *mbar = reinterpret_cast<uint64_t *>(sm + win_bytes);
+  unsigned *bits = reinterpret_cast<unsigned *>(sm + win_bytes + 16);
+  if (kSmem && threadIdx.x == 0) {
+    mbar_init(mbar, 1);
+    mbar_expect_tx(mbar, win_bytes);
+    for (int b = 0; b < a.nboxes; b++)
+      tma_load_2d(win + (size_t)b * a.box_rows * a.win_w, &map, hy0, hx0 + b * a.box_rows, mbar);
+  }
+  for (int i = threadIdx.x; i < 2 * nwords; i += blockDim.x) bits[i] = 0u;
+  __syncthreads();
+  if (threadIdx.x == 0) shed_set(bits, nwpr, a.roi, a.roi);  // siting.cpp:279
+  if (kSmem) {
+    if (!mbar_wait(mbar, 0)) {
+      if (threadIdx.x == 0) atomicOr(a.err, kErrTmaTimeout);
+      return;
+    }
+    sweep_rays(SmemDem{win, a.win_w, hx0, hy0}, a, ox, oy, bits);
+  } else {
+    sweep_rays(GlobalDem{a.dem, a.pitch}, a, ox, oy, bits);
+  }
+  __syncthreads();
+  uint64_t *dst = a.sheds + (size_t)blockIdx.x * nwords;
+  const uint64_t *src = reinterpret_cast<const uint64_t *>(bits);
+  for (int i = threadIdx.x; i < nwords; i += blockDim.x) dst[i] = src[i];
+}
+
+int round8(int v) { return (v + 7) & ~7; }
+
+struct WinGeom {
+  int w, box_rows, nboxes;
+};
+
+WinGeom win_geom(int roi) {
+  WinGeom g;
+  const int nr = 2 * roi + 1;
+  g.w = round8(2 * roi + 8);
+  g.nboxes = (nr + 255) / 256;
+  g.box_rows = round8((nr + g.nboxes - 1) / g.nboxes);
+  return g;
+}
+
+}  // namespace
+
+size_t shed_smem_bytes(const ShedPlan &p, int roi) {
+  const int nr = 2 * roi + 1, nwpr = (nr + 63) / 64;
+  size_t b = 16 + (size_t)nr * nwpr * 8;
+  if (p.use_smem) {
+    const WinGeom g = win_geom(roi);
+    b += (size_t)g.nboxes * g.box_rows * g.w * 2;
+  }
+  return b;
+}
+
+ShedPlan shed_default_plan(int roi) {
+  ShedPlan p{256, true};
+  const WinGeom g = win_geom(roi);
+  if (g.w > 256 || shed_smem_bytes(p, roi) > 110 * 1024) p.use_smem = false;
+  return p;
+}
+
+cudaError_t launch_sheds(const DemView &dem, int roi, int oht, int tht, int nsheds,
+                         const int32_t *obs, uint64_t *sheds, const ShedPlan &plan, int *d_err,
+                         cudaStream_t st) {
+  if (nsheds <= 0) return cudaSuccess;
+  ShedArgs a{};
+  a.dem = dem.data;
+  a.pitch = dem.pitch;
+  a.n = dem.nrows;
+  a.roi = roi;
+  a.oht = oht;
+  a.tht = tht;
+  a.nsheds = nsheds;
+  a.obs = obs;
+  a.sheds = sheds;
+  a.err = d_err;
+  CUtensorMap map;
+  memset(&map, 0, sizeof(map));
+  const bool smem = plan.use_smem && dem.tma_ok;
+  if (smem) {
+    const WinGeom g = win_geom(roi);
+    a.win_w = g.w;
+    a.box_rows = g.box_rows;
+    a.nboxes = g.nboxes;
+    if (!make_dem_tensor_map(&map, dem, g.w, g.box_rows)) return cudaErrorInvalidValue;
+  }
+  ShedPlan eff = plan;
+  eff.use_smem = smem;
+  const size_t shm = shed_smem_bytes(eff, roi);
+  cudaError_t e;
+  if (smem) {
+    e = cudaFuncSetAttribute(shed_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)shm);
+    if (e != cudaSuccess) return e;
+    shed_kernel<true><<<nsheds, plan.threads, shm, st>>>(map, a);
+  } else {
+    e = cudaFuncSetAttribute(shed_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)shm);
+    if (e != cudaSuccess) return e;
+    shed_kernel<false><<<nsheds, plan.threads, shm, st>>>(map, a);
+  }
+  return cudaGetLastError();
+}
+
+}  // namespace siting

@@ -1,0 +1,301 @@
+// VIX: approximate visibility index of every DEM cell (siting.cpp:137-198).
+//
+// Each cell tests `ntests` random targets within roi; a target is visible when
+// no sampled ground point on the line of sight (offsets 1,2,4,8,... along the
+// major axis) rises above the sight line.  VIX = min(255, (int)(nvis/ntests *
+// 255.999f)).
+//
+// GB300 mapping: one CTA per T x T cell tile.  The tile's halo (T+2roi rows,
+// T+2roi+7 columns rounded to 8) is loaded into shared memory by one TMA
+// bulk-tensor copy, so every line-of-sight sample is a shared-memory gather.
+// Warps split the tile's cells evenly and walk the flat (cell, target) space
+// 32 items at a time; the target of item (cell, t) comes from the LCG state
+// after 2t+1 steps from the seed, obtained by an affine jump-ahead table
+// instead of a serial chain.  Per-cell hit counts accumulate in shared memory
+// and become VIX bytes through a host-computed table.  When the halo does not
+// fit a single TMA box (large roi) the same code reads the DEM through the
+// read-only L1 path instead.
+//
+// Bit-exactness: every FP32 operation is separately rounded (no FMA), the
+// reference's drecip = (float)(1.0/d) comes from a host table, and C's
+// truncating integer division and round-half-away-from-zero are kept.
+#include <algorithm>
+
+#include "common.cuh"
+#include "kernels.h"
+
+namespace siting {
+namespace {
+
+struct VixArgs {
+  const uint16_t *dem;
+  int pitch, n, roi, oht, tht, ntests;
+  uint8_t *vix;
+  int tile, tiles_per_row;
+  int halo_w, box_rows, nboxes;
+  const uint32_t *jump;  // ntests pairs: LCG map of 2t+1 steps
+  const float *rtab;     // roi+1
+  const uint8_t *vtab;   // ntests+1
+  int *err;
+};
+
+struct SmemDem {
+  const uint16_t *s;
+  int w, x0, y0;
+  __device__ __forceinline__ int at(int x, int y) const { return s[(x - x0) * w + (y - y0)]; }
+};
+
+struct GlobalDem {
+  const uint16_t *g;
+  int pitch;
+  __device__ __forceinline__ int at(int x, int y) const { return __ldg(g + x * pitch + y); }
+};
+
+// One random target of one cell (siting.cpp:155-175 and 54-135).
+template <class Dem>
+__device__ __forceinline__ int vix_target(const Dem &dem, int n, int roi, int roi2, int tht,
+                                          float span, int ox, int oy, int oz, float foz,
+                                          uint32_t r1, const float *rtab) {
+  const uint32_t r2 = lcg_step(r1);
+  // (int)((2*roi+0.99999f)*r/RANDOM_MAX): the divisor is 2^31, so a multiply
+  // by 2^-31 is the same exactly-rounded result.
+  int dx = f2i(fmul(fmul(span, i2f((int)r1)), 0x1p-31f)) - roi;
+  int dy = f2i(fmul(fmul(span, i2f((int)r2)), 0x1p-31f)) - roi;
+  if (dx * dx + dy * dy > roi2) {  // fold into the circle (siting.cpp:162-166)
+    dx /= 3;
+    dy /= 3;
+  }
+  const int tx = ox + dx, ty = oy + dy;
+  if ((unsigned)tx >= (unsigned)n || (unsigned)ty >= (unsigned)n) return 0;
+  const int adx = abs(dx), ady = abs(dy);
+  if (adx <= 1 && ady <= 1) return 1;
+  const int tz = dem.at(tx, ty) + tht;
+  const bool mx = adx >= ady;
+  const int d = mx ? dx : dy, m = mx ? dy : dx, ad = mx ? adx : ady;
+  const float rr = rtab[ad];
+  const float drecip = d > 0 ? rr : -rr;
+  const float slope = fmul(i2f(m), drecip);
+  const float zslope = fmul(i2f(tz - oz), drecip);
+  const int sg = d > 0 ? 1 : -1;
+  for (int step = 1; step < ad; step <<= 1) {
+    const int id = sg * step;
+    const float fid = i2f(id);
+    const int off = round_i(fmul(slope, fid));
+    const int x = mx ? ox + id : ox + off;
+    const int y = mx ? oy + off : oy + id;
+    if (i2f(dem.at(x, y)) > fadd(foz, fmul(fid, zslope))) return 0;
+  }
+  return 1;
+}
+
+template <class Dem>
+__device__ __forceinline__ void vix_tile_work(const Dem &dem, const VixArgs &a, int tx0, int ty0,
+                                              const uint2 *jump, const float *rtab, int *cnt) {
+  const int T = a.tile, ncell = T * T;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  const int cb = warp * ncell / nw, ce = (warp + 1) * ncell / nw;
+  const float span = fadd(i2f(2 * a.roi), 0.99999f);
+  const int roi2 = a.roi * a.roi;
+  int cell = cb + lane / a.ntests, t = lane % a.ntests;
+  int cur = -1, acc = 0, ox = 0, oy = 0, oz = 0;
+  uint32_t seed = 0;
+  float foz = 0.f;
+  bool valid = false;
+  while (cell < ce) {
+    if (cell != cur) {
+      if (acc) atomicAdd(&cnt[cur], acc);
+      cur = cell;
+      acc = 0;
+      const int lx = cell / T;
+      ox = tx0 + lx;
+      oy = ty0 + (cell - lx * T);
+      valid = ox < a.n && oy < a.n;
+      if (valid) {
+        oz = dem.at(ox, oy) + a.oht;
+        foz = i2f(oz);
+        seed = (uint32_t)(ox * a.n + oy);
+      }
+    }
+    if (valid) {
+      const uint2 j = jump[t];
+      const uint32_t r1 = (j.x * seed + j.y) & 0x7fffffffu;
+      acc += vix_target(dem, a.n, a.roi, roi2, a.tht, span, ox, oy, oz, foz, r1, rtab);
+    }
+    t += 32;
+    while (t >= a.ntests) {
+      t -= a.ntests;
+      cell++;
+    }
+  }
+  if (acc) atomicAdd(&cnt[cur], acc);
+}
+
+template <bool kSmem>
+__global__ void __launch_bounds__(512) vix_kernel(const __grid_constant__ CUtensorMap map,
+                                                  const VixArgs a) {
+  extern __shared__ __align__(128) unsigned char sm[];
+  const int T = a.tile;
+  const int tx0 = (blockIdx.x / a.tiles_per_row) * T;
+  const int ty0 = (blockIdx.x % a.tiles_per_row) * T;
+  const int hx0 = tx0 - a.roi;
+  const int hy0 = (ty0 - a.roi) & ~7;  // TMA inner coordinate: 16-byte aligned
+  size_t off = 0;
+  uint16_t *halo = reinterpret_cast<uint16_t *>(sm);
+  const uint32_t halo_bytes = kSmem ? (uint32_t)a.nboxes * a.box_rows * a.halo_w * 2u : 0u;
+  off += halo_bytes;
+  uint64_t *mbar = reinterpret_cast<uint64_t *>(sm + off);
+  off += 16;
+  uint2 *jump = reinterpret_cast<uint2 *>(sm + off);
+  off += (size_t)a.ntests * 8;
+  float *rtab = reinterpret_cast<float *>(sm + off);
+  off += (size_t)(a.roi + 1) * 4;
+  int *cnt = reinterpret_cast<int *>(sm + off);
+  off += (size_t)T * T * 4;
+  uint8_t *vtab = sm + off;
+
+  if (kSmem && threadIdx.x == 0) {
+    mbar_init(mbar, 1);
+    mbar_expect_tx(mbar, halo_bytes);
+    for (int b = 0; b < a.nboxes; b++)
+      tma_load_2d(halo + (size_t)b * a.box_rows * a.halo_w, &map, hy0, hx0 + b * a.box_rows,
+                  mbar);
+  }
+  for (int i = threadIdx.x; i < a.ntests; i += blockDim.x)
+    jump[i] = make_uint2(a.jump[2 * i], a.jump[2 * i + 1]);
+  for (int i = threadIdx.x; i <= a.roi; i += blockDim.x) rtab[i] = a.rtab[i];
+  for (int i = threadIdx.x; i <= a.ntests; i += blockDim.x) vtab[i] = a.vtab[i];
+  for (int i = threadIdx.x; i < T * T; i += blockDim.x) cnt[i] = 0;
+  __syncthreads();
+
+  if (kSmem) {
+    if (!mbar_wait(mbar, 0)) {
+      if (threadIdx.x == 0) atomicOr(a.err, kErrTmaTimeout);
+      return;
+    }
+    vix_tile_work(SmemDem{halo, a.halo_w, hx0, hy0}, a, tx0, ty0, jump, rtab, cnt);
+  } else {
+    vix_tile_work(GlobalDem{a.dem, a.pitch}, a, tx0, ty0, jump, rtab, cnt);
+  }
+  __syncthreads();
+  for (int i = threadIdx.x; i < T * T; i += blockDim.x) {
+    const int lx = i / T;
+    const int x = tx0 + lx, y = ty0 + (i - lx * T);
+    if (x < a.n && y < a.n) a.vix[x * a.n + y] = vtab[cnt[i]];
+  }
+}
+
+int round8(int v) { return (v + 7) & ~7; }
+
+struct HaloGeom {
+  int w, box_rows, nboxes;
+};
+
+HaloGeom halo_geom(int tile, int roi) {
+  HaloGeom g;
+  g.w = round8(tile + 2 * roi + 7);
+  const int h = tile + 2 * roi;
+  g.nboxes = (h + 255) / 256;
+  g.box_rows = round8((h + g.nboxes - 1) / g.nboxes);
+  return g;
+}
+
+size_t tables_tail_bytes(int tile, int roi, int ntests) {
+  return 16 + (size_t)ntests * 8 + (size_t)(roi + 1) * 4 + (size_t)tile * tile * 4 + ntests + 1;
+}
+
+}  // namespace
+
+size_t vix_table_bytes(int roi, int ntests) {
+  return (((size_t)ntests * 8 + (size_t)(roi + 1) * 4 + ntests + 1) + 15) & ~(size_t)15;
+}
+
+void vix_fill_tables(void *host_buf, int roi, int ntests) {
+  uint32_t *jump = static_cast<uint32_t *>(host_buf);
+  const uint32_t a = 1103515245u, c = 12345u;
+  uint32_t A = a, C = c;  // map of 1 step
+  for (int t = 0; t < ntests; t++) {
+    jump[2 * t] = A;  // map of 2t+1 steps
+    jump[2 * t + 1] = C;
+    A = a * (a * A);  // advance by two steps
+    C = a * (a * C + c) + c;
+  }
+  float *rtab = reinterpret_cast<float *>(jump + 2 * ntests);
+  rtab[0] = 0.f;
+  for (int d = 1; d <= roi; d++) rtab[d] = (float)(1.0 / d);  // siting.cpp:91
+  uint8_t *vtab = reinterpret_cast<uint8_t *>(rtab + roi + 1);
+  for (int v = 0; v <= ntests; v++) {
+    const float f = (float)v / ntests;  // siting.cpp:186-189
+    const int q = (int)(f * 255.999f);
+    vtab[v] = (uint8_t)(q < 255 ? q : 255);
+  }
+}
+
+size_t vix_smem_bytes(const VixPlan &p, int roi, int ntests) {
+  size_t b = tables_tail_bytes(p.tile, roi, ntests);
+  if (p.use_smem) {
+    const HaloGeom g = halo_geom(p.tile, roi);
+    b += (size_t)g.nboxes * g.box_rows * g.w * 2;
+  }
+  return b;
+}
+
+VixPlan vix_default_plan(int nrows, int roi, int ntests) {
+  (void)nrows;
+  VixPlan p{32, 512, false};
+  const size_t limit = 220 * 1024;
+  for (int tile : {64, 32, 16}) {
+    VixPlan q{tile, 512, true};
+    const HaloGeom g = halo_geom(tile, roi);
+    if (g.w <= 256 && vix_smem_bytes(q, roi, ntests) <= limit) return q;
+  }
+  if (vix_smem_bytes(p, roi, ntests) > limit) p.tile = 16;
+  return p;
+}
+
+cudaError_t launch_vix(const DemView &dem, int roi, int oht, int tht, int ntests, uint8_t *vix,
+                       const void *d_tables, const VixPlan &plan, int *d_err, cudaStream_t st) {
+  VixArgs a{};
+  a.dem = dem.data;
+  a.pitch = dem.pitch;
+  a.n = dem.nrows;
+  a.roi = roi;
+  a.oht = oht;
+  a.tht = tht;
+  a.ntests = ntests;
+  a.vix = vix;
+  a.tile = plan.tile;
+  a.tiles_per_row = ceil_div(dem.nrows, plan.tile);
+  a.jump = static_cast<const uint32_t *>(d_tables);
+  a.rtab = reinterpret_cast<const float *>(a.jump + 2 * ntests);
+  a.vtab = reinterpret_cast<const uint8_t *>(a.rtab + roi + 1);
+  a.err = d_err;
+  CUtensorMap map;
+  memset(&map, 0, sizeof(map));
+  const bool smem = plan.use_smem && dem.tma_ok;
+  if (smem) {
+    const HaloGeom g = halo_geom(plan.tile, roi);
+    a.halo_w = g.w;
+    a.box_rows = g.box_rows;
+    a.nboxes = g.nboxes;
+    if (!make_dem_tensor_map(&map, dem, g.w, g.box_rows)) return cudaErrorInvalidValue;
+  }
+  VixPlan eff = plan;
+  eff.use_smem = smem;
+  const size_t shm = vix_smem_bytes(eff, roi, ntests);
+  const int grid = a.tiles_per_row * a.tiles_per_row;
+  cudaError_t e;
+  if (smem) {
+    e = cudaFuncSetAttribute(vix_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)shm);
+    if (e != cudaSuccess) return e;
+    vix_kernel<true><<<grid, plan.threads, shm, st>>>(map, a);
+  } else {
+    e = cudaFuncSetAttribute(vix_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)shm);
+    if (e != cudaSuccess) return e;
+    vix_kernel<false><<<grid, plan.threads, shm, st>>>(map, a);
+  }
+  return cudaGetLastError();
+}
+
+}  // namespace siting
