@@ -1,0 +1,338 @@
+"""Benchmark: DEM cells/s of the VIX -> FINDMAX -> VIEWSHED -> SITE pipeline.
+
+Workload (default): one 4096 x 4096 uint16 DEM, seeded fBm (10 octaves,
+persistence 0.5, lacunarity 2, base wavelength 256) blended with ridged noise
+at weight 0.3, range 0-30000; roi=100, height=200, targets=100, bw=16,
+nwanted=65536, intervis=1.
+
+One step = one whole siting job.  `value` is n^2 / device time with the DEM
+resident in HBM (siting_run_dev); `e2e` is the same metric through
+siting_run with page-locked host buffers (DEM upload and observer/selection
+download inside the timed region).  Between timed steps the L2 is flushed by
+writing a 512 MiB buffer.  Under torchrun each rank runs an independent
+replica (its own DEM seed): value = all ranks' cells / max rank time.
+
+`--impl reference` times the CPU implementation of the same pipeline (the
+reference built from its sources where available, else the oracle port) on
+the host's cores, on a bounded sample of the workload.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+WORKLOADS = {
+    "c2_4096": dict(nrows=4096, roi=100, height=200, ntests=100, bw=16, nwanted0=65536,
+                    intervis=1, octaves=10, ridged=0.3, range_max=30000, seed=4096),
+    "c1_1000": dict(nrows=1000, roi=50, height=100, ntests=50, bw=10, nwanted0=10000,
+                    intervis=0, octaves=8, ridged=0.0, range_max=10000, seed=1000),
+    "c4_16384": dict(nrows=16384, roi=200, height=150, ntests=64, bw=32, nwanted0=262144,
+                     intervis=0, octaves=12, ridged=0.0, range_max=40000, seed=16384),
+}
+METRIC = "DEM cells/s end-to-end"
+
+
+def make_dem(w, seed_offset=0):
+    import siting_gb300 as sg
+
+    return sg.fbm_dem(w["nrows"], w["seed"] + seed_offset, octaves=w["octaves"],
+                      ridged_weight=w["ridged"], range_max=w["range_max"])
+
+
+def params(w):
+    import siting_gb300 as sg
+
+    return sg.Params(nrows=w["nrows"], roi=w["roi"], height=w["height"], ntests=w["ntests"],
+                     bw=w["bw"], nwanted0=w["nwanted0"], intervis=w["intervis"])
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.Q}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except FileNotFoundError:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        self.t.join(timeout=2)
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 8:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax.append(float(f[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[4:8]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(smax) if smax else None,
+                "samples": len(sm), "reasons": sorted(reasons)}
+
+
+def site_algorithmic_bytes(nrows, roi, obs, order, nsheds):
+    """Reference SITE traffic (the rescoring work of siting.cpp:537-604).
+
+    Sum over rounds of, for every rescored candidate, its shed (nr*nwpr words)
+    plus its coverage window (nr*(lastword-firstword+1) words), plus per pick
+    the union's read-modify-write (2*nr*(nwpr+1) words) and the area/used
+    scan (nwanted*(4+1) bytes)."""
+    nr = 2 * roi + 1
+    nwpr = (nr + 63) // 64
+    x = (obs // nrows).astype(np.int64)
+    y = (obs % nrows).astype(np.int64)
+    fw = np.floor_divide(y - roi, 64)
+    lw = (y + roi) // 64
+    per_cand = (nr * nwpr + nr * (lw - fw + 1)) * 8
+    used = np.zeros(nsheds, bool)
+    total = int(per_cand.sum())  # round 1: every candidate
+    lim = 4 * roi * roi
+    for t, p in enumerate(order):
+        used[p] = True
+        total += 2 * nr * (nwpr + 1) * 8 + nsheds * 5
+        if t + 1 < len(order):  # the next round rescores neighbours of p
+            m = (~used) & ((x - x[p]) ** 2 + (y - y[p]) ** 2 <= lim)
+            total += int(per_cand[m].sum())
+    return total
+
+
+def run_gpu(args, w):
+    import torch
+
+    import siting_gb300 as sg
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl")
+    n = w["nrows"]
+    p = params(w)
+    g = sg.block_geometry(n, w["bw"], w["nwanted0"])
+    dem = make_dem(w, seed_offset=rank)
+    ctx = sg.Context(local)
+    stream = torch.cuda.ExternalStream(ctx.stream)
+
+    # device-resident buffers
+    d_dem = torch.from_numpy(dem.view(np.int16)).to(f"cuda:{local}")
+    d_obs = torch.empty(g.nwanted, dtype=torch.int32, device=f"cuda:{local}")
+    d_sel = torch.empty(g.nwanted, dtype=torch.uint8, device=f"cuda:{local}")
+    # pinned host buffers for the end-to-end form
+    h_dem = torch.from_numpy(dem.view(np.int16)).pin_memory()
+    h_obs = torch.empty(g.nwanted, dtype=torch.int32).pin_memory()
+    h_sel = torch.empty(g.nwanted, dtype=torch.uint8).pin_memory()
+    flush = torch.empty(512 << 20, dtype=torch.uint8, device=f"cuda:{local}")
+    torch.cuda.synchronize()
+
+    def barrier():
+        if world > 1:
+            import torch.distributed as dist
+
+            dist.barrier()
+
+    def timed(fn):
+        flush.zero_()
+        torch.cuda.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        r = fn()
+        e1.record(stream)
+        e1.synchronize()
+        return e0.elapsed_time(e1), r
+
+    dev_step = lambda: ctx.run_dev(p, d_dem, d_obs, d_sel)  # noqa: E731
+    e2e_step = lambda: ctx.run_into(p, h_dem, h_obs, h_sel)  # noqa: E731
+
+    for _ in range(args.warmup):
+        timed(dev_step)
+        timed(e2e_step)
+    clocks = ClockSampler(local)
+    barrier()
+    torch.cuda.synchronize()
+    clocks.start()
+    dev_ms, e2e_ms, stage = [], [], []
+    for _ in range(args.steps):
+        ms, r = timed(dev_step)
+        dev_ms.append(ms)
+        stage.append(r)
+    for _ in range(args.steps):
+        ms, _ = timed(e2e_step)
+        e2e_ms.append(ms)
+    torch.cuda.synchronize()
+    barrier()
+    clk = clocks.stop()
+
+    mean_dev = sum(dev_ms) / len(dev_ms)
+    mean_e2e = sum(e2e_ms) / len(e2e_ms)
+    if world > 1:
+        import torch.distributed as dist
+
+        t = torch.tensor([mean_dev, mean_e2e], device=f"cuda:{local}")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        mean_dev, mean_e2e = t.tolist()
+    r = stage[-1]
+    out = {
+        "metric": METRIC, "value": world * n * n / (mean_dev / 1e3), "unit": "cells/s",
+        "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": mean_dev, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32/u64", "data": "synthetic",
+        "config": {"workload": args.workload, "nrows": n, "roi": w["roi"],
+                   "height": w["height"], "targets": w["ntests"], "bw": w["bw"],
+                   "nwanted": g.nwanted, "intervis": w["intervis"],
+                   "dem": f"fbm {w['octaves']} octaves, ridged {w['ridged']}, 0-{w['range_max']}",
+                   "parallelism": f"replicas{world}", "l2": "flushed (512 MiB write) between steps"},
+        "e2e": {"value": world * n * n / (mean_e2e / 1e3), "unit": "cells/s",
+                "ms_per_step": mean_e2e, "h2d_bytes_per_step": n * n * 2,
+                "d2h_bytes_per_step": g.nwanted * 5},
+        "gpu_launches": 4 * args.steps,
+        "observers_per_s": world * g.nwanted / (mean_dev / 1e3),
+        "stages_ms": {"vix": r.ms_vix, "findmax": r.ms_findmax, "viewshed": r.ms_viewshed,
+                      "site": r.ms_site},
+        "site": {"nusedsheds": r.nusedsheds, "coverage": r.coverage, "rounds": r.site_rounds},
+        "clocks": clk,
+    }
+    return out, (dem, d_obs, d_sel, r, ctx, g)
+
+
+def roofline(out, w, state, peaks):
+    """Roofline of the dominant stage; also the SITE HBM figure."""
+    dem, d_obs, d_sel, r, ctx, g = state
+    n, roi = w["nrows"], w["roi"]
+    hbm = peaks.get("hbm_gbs", 6800.0)
+    src = "measured" if "hbm_gbs" in peaks else "fallback"
+    obs = d_obs.cpu().numpy()
+    order = ctx.last_pick_order(g.nwanted)
+    st = out["stages_ms"]
+    res = {}
+    if order is not None:
+        b = site_algorithmic_bytes(n, roi, obs, order, g.nwanted)
+        ach = b / (st["site"] / 1e3) / 1e9
+        res["site"] = {"bound": "hbm", "achieved": ach, "peak": hbm, "unit": "GB/s",
+                       "frac": ach / hbm, "alg_bytes": b}
+    return res, src
+
+
+def run_reference(args, w):
+    """CPU implementation of the pipeline on a bounded sample of the workload."""
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    from oracle_bind import Oracle, reference_available
+
+    kind = "reference_omp" if reference_available() and os.path.exists(
+        os.path.join(ROOT, "oracle", "_ref", "libsitingref_omp.so")) else "port"
+    orc = Oracle(kind if kind == "port" else "reference_omp")
+    if kind == "port":
+        orc.lib.oracle_set_threads(os.cpu_count() or 1)
+    rows = min(args.cpu_sample_rows, w["nrows"])
+    full = make_dem(w)
+    sample = full.reshape(w["nrows"], w["nrows"])[:rows, :rows].copy().ravel()
+    nw = max(1, int(w["nwanted0"] * (rows / w["nrows"]) ** 2))
+    times = []
+    for i in range(args.warmup + args.steps):
+        t0 = time.perf_counter()
+        orc.run(sample, rows, w["roi"], w["height"], w["ntests"], w["bw"], nw, w["intervis"])
+        dt = time.perf_counter() - t0
+        if i >= args.warmup:
+            times.append(dt)
+    mean = sum(times) / len(times)
+    cores = os.cpu_count() or 1
+    return {"kind": "reference" if kind != "port" else "port", "value": rows * rows / mean,
+            "unit": "cells/s", "cores": cores, "seconds_per_step": mean,
+            "sample": f"{rows}x{rows} corner of the {w['nrows']}^2 workload DEM, same parameters, "
+                      f"nwanted scaled to {nw}; whole pipeline"}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--workload", default="c2_4096", choices=sorted(WORKLOADS))
+    ap.add_argument("--cpu-sample-rows", type=int, default=2048)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    w = WORKLOADS[args.workload]
+    rank = int(os.environ.get("RANK", "0"))
+
+    if args.impl == "reference":
+        if rank != 0:
+            return
+        cb = run_reference(args, w)
+        line = {"metric": METRIC, "value": cb["value"], "unit": "cells/s", "n_gpus": args.gpus,
+                "steps": args.steps, "warmup": args.warmup,
+                "ms_per_step": cb["seconds_per_step"] * 1e3, "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "f32/u64", "data": "synthetic",
+                "config": {"workload": args.workload, "sample": cb["sample"]},
+                "impl": "reference",
+                "cpu_baseline": {k: cb[k] for k in ("value", "unit", "cores", "kind", "sample")},
+                "e2e": {"value": cb["value"], "unit": "cells/s", "h2d_bytes_per_step": 0,
+                        "d2h_bytes_per_step": 0}}
+        print(json.dumps(line))
+        return
+
+    out, state = run_gpu(args, w)
+    if rank != 0:
+        return
+    peaks = {}
+    pp = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(pp):
+        with open(pp) as f:
+            peaks = json.load(f)
+    rl, src = roofline(out, w, state, peaks)
+    out["roofline_stages"] = rl
+    out["peak_source"] = src
+    if not args.no_cpu_baseline and int(os.environ.get("WORLD_SIZE", "1")) == 1:
+        cb = run_reference(argparse.Namespace(warmup=0, steps=1,
+                                              cpu_sample_rows=args.cpu_sample_rows), w)
+        out["cpu_baseline"] = {k: cb[k] for k in ("value", "unit", "cores", "kind", "sample")}
+    print(json.dumps(out))
+
+
+if __name__ == "__main__":
+    main()

@@ -144,6 +144,12 @@ int siting_site_it_dev(siting_ctx *ctx, int nrows, int roi, int intervis,
                        const uint64_t *d_sheds, uint8_t *d_selected,
                        siting_result *res);
 
+/* Picks of the context's last SITE run in the order they were made (the
+ * sequence the reference's commented-out per-round log prints,
+ * siting.cpp:610-615).  Writes min(cap, nusedsheds) entries to order (host)
+ * and returns that count in *count. */
+int siting_last_pick_order(siting_ctx *ctx, int32_t *order, int cap, int *count);
+
 /* ---- whole pipeline (replaces main's stage sequence, siting.cpp:737-759).
  * obs and selected receive nwanted entries (see siting_block_geometry). --- */
 int siting_run(siting_ctx *ctx, const siting_params *p, const uint16_t *elevs,

@@ -140,6 +140,7 @@ def load() -> C.CDLL:
         "siting_site_it_dev": ([_P, i, i, i, i, _P, _P, _P, C.POINTER(_ResultC)], i),
         "siting_run": ([_P, C.POINTER(_ParamsC), _P, _P, _P, C.POINTER(_ResultC)], i),
         "siting_run_dev": ([_P, C.POINTER(_ParamsC), _P, _P, _P, C.POINTER(_ResultC)], i),
+        "siting_last_pick_order": ([_P, _P, i, C.POINTER(C.c_int)], i),
         "siting_read_dem": ([C.c_char_p, i, _P], i),
         "siting_write_observers": ([C.c_char_p, i, i, _P, _P], i),
         "siting_fbm_dem": ([_P, i, C.c_uint64, i, C.c_double, C.c_double, C.c_double,
@@ -323,6 +324,13 @@ class Context:
         self._check(self._lib.siting_site_it_dev(self.h, nrows, roi, intervis, nsheds, _ptr(d_obs),
                                                  _ptr(d_sheds), _ptr(d_selected), C.byref(r)))
         return Result.of(r)
+
+    def last_pick_order(self, cap: int) -> np.ndarray:
+        """Candidate indices of the last SITE run, in pick order."""
+        out = np.empty(max(cap, 0), np.int32)
+        cnt = C.c_int()
+        self._check(self._lib.siting_last_pick_order(self.h, out.ctypes.data, cap, C.byref(cnt)))
+        return out[:cnt.value]
 
     # ---- whole pipeline ---------------------------------------------------------
     def run(self, p: Params, elevs):

@@ -41,6 +41,8 @@ struct siting_ctx {
   int tab_roi = -1, tab_ntests = -1;  // VIX tables currently on the device
   std::vector<unsigned char> tab_host;
   long long *h_out = nullptr;  // pinned: SITE outputs + error flag
+  int32_t *d_last_order = nullptr;  // pick order of the last SITE run (in kSite)
+  int last_nused = 0;
 };
 
 namespace {
@@ -228,11 +230,13 @@ int site_enqueue(siting_ctx *ctx, int nrows, int roi, int intervis, int nsheds,
                  d_err, ctx->stream));
   CK(cudaMemcpyAsync(ctx->h_out, s.out, 3 * sizeof(long long), cudaMemcpyDeviceToHost,
                      ctx->stream));
+  ctx->d_last_order = s.order;
   return SITING_OK;
 }
 
 // After a stream sync: SITE outputs into res (nusedsheds, cumarea, coverage).
 void site_collect(siting_ctx *ctx, int nrows, siting_result *res) {
+  ctx->last_nused = (int)ctx->h_out[0];
   if (!res) return;
   res->nusedsheds = (int)ctx->h_out[0];
   res->cumarea = ctx->h_out[1];
@@ -361,6 +365,8 @@ int siting_ctx_trim(siting_ctx *ctx) {
     b = DevBuf{};
   }
   ctx->held = 0;
+  ctx->d_last_order = nullptr;
+  ctx->last_nused = 0;
   return SITING_OK;
 }
 
@@ -562,6 +568,18 @@ int siting_site_it(siting_ctx *ctx, int nrows, int roi, int intervis, int nsheds
     return rc;
   if (nsheds) CK(cudaMemcpyAsync(selected, d_sel, nsheds, cudaMemcpyDeviceToHost, ctx->stream));
   CK(cudaStreamSynchronize(ctx->stream));
+  return SITING_OK;
+}
+
+int siting_last_pick_order(siting_ctx *ctx, int32_t *order, int cap, int *count) {
+  if (!ctx || !count || cap < 0 || (cap && !order)) return SITING_EINVAL;
+  const int n = std::min(cap, ctx->last_nused);
+  *count = ctx->d_last_order ? n : 0;
+  if (ctx->d_last_order && n > 0) {
+    CK(cudaMemcpyAsync(order, ctx->d_last_order, (size_t)n * 4, cudaMemcpyDeviceToHost,
+                       ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+  }
   return SITING_OK;
 }
 

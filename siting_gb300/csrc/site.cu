@@ -220,18 +220,15 @@ __global__ void __launch_bounds__(kSiteThreads, 1) site_kernel(const SiteArgs a)
         const int prow = i / nbw, j = i - prow * nbw;
         uint64_t v = ncur[i];
         int gr = px - roi + prow, W = fw + j;
-        if (v && gr >= 0 && gr < n && W >= 0 && W < cw) {
-          uint64_t *dst = Y + (size_t)gr * cw + W;
-          __stcg(dst, __ldcg(dst) | v);
-        }
+        // the two windows overlap when the picks are within 2*roi: OR atomically
+        if (v && gr >= 0 && gr < n && W >= 0 && W < cw)
+          atomicOr(reinterpret_cast<unsigned long long *>(Y + (size_t)gr * cw + W), v);
         if (have_prev) {
           v = nprev[i];
           gr = prev_px - roi + prow;
           W = prev_fw + j;
-          if (v && gr >= 0 && gr < n && W >= 0 && W < cw) {
-            uint64_t *dst = Y + (size_t)gr * cw + W;
-            __stcg(dst, __ldcg(dst) | v);
-          }
+          if (v && gr >= 0 && gr < n && W >= 0 && W < cw)
+            atomicOr(reinterpret_cast<unsigned long long *>(Y + (size_t)gr * cw + W), v);
         }
       }
     }
