@@ -35,6 +35,8 @@ sys.path.insert(0, ROOT)
 WORKLOADS = {
     "c2_4096": dict(nrows=4096, roi=100, height=200, ntests=100, bw=16, nwanted0=65536,
                     intervis=1, octaves=10, ridged=0.3, range_max=30000, seed=4096),
+    "c2_2048": dict(nrows=2048, roi=100, height=200, ntests=100, bw=16, nwanted0=16384,
+                    intervis=1, octaves=10, ridged=0.3, range_max=30000, seed=2048),
     "c1_1000": dict(nrows=1000, roi=50, height=100, ntests=50, bw=10, nwanted0=10000,
                     intervis=0, octaves=8, ridged=0.0, range_max=10000, seed=1000),
     "c4_16384": dict(nrows=16384, roi=200, height=150, ntests=64, bw=32, nwanted0=262144,
@@ -234,7 +236,8 @@ def run_gpu(args, w):
         "observers_per_s": world * g.nwanted / (mean_dev / 1e3),
         "stages_ms": {"vix": r.ms_vix, "findmax": r.ms_findmax, "viewshed": r.ms_viewshed,
                       "site": r.ms_site},
-        "site": {"nusedsheds": r.nusedsheds, "coverage": r.coverage, "rounds": r.site_rounds},
+        "site": {"nusedsheds": r.nusedsheds, "coverage": r.coverage, "rounds": r.site_rounds,
+                 "phase_cycles": ctx.last_site_phase_cycles()},
         "clocks": clk,
     }
     return out, (dem, d_obs, d_sel, r, ctx, g)

@@ -150,6 +150,12 @@ int siting_site_it_dev(siting_ctx *ctx, int nrows, int roi, int intervis,
  * and returns that count in *count. */
 int siting_last_pick_order(siting_ctx *ctx, int32_t *order, int cap, int *count);
 
+/* Tracing: device clock cycles CTA 0 spent in each phase of the last SITE
+ * run (0 initial scores, 1 max-tree refresh + publish, 2 group barrier,
+ * 3 agreeing on the pick, 4 new bits + neighbour search, 5 gain deltas,
+ * 6 intervis gate and updates).  Writes min(n, 7) values. */
+int siting_last_site_phase_cycles(siting_ctx *ctx, long long *cycles, int n);
+
 /* ---- whole pipeline (replaces main's stage sequence, siting.cpp:737-759).
  * obs and selected receive nwanted entries (see siting_block_geometry). --- */
 int siting_run(siting_ctx *ctx, const siting_params *p, const uint16_t *elevs,

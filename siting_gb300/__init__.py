@@ -141,6 +141,7 @@ def load() -> C.CDLL:
         "siting_run": ([_P, C.POINTER(_ParamsC), _P, _P, _P, C.POINTER(_ResultC)], i),
         "siting_run_dev": ([_P, C.POINTER(_ParamsC), _P, _P, _P, C.POINTER(_ResultC)], i),
         "siting_last_pick_order": ([_P, _P, i, C.POINTER(C.c_int)], i),
+        "siting_last_site_phase_cycles": ([_P, _P, i], i),
         "siting_read_dem": ([C.c_char_p, i, _P], i),
         "siting_write_observers": ([C.c_char_p, i, i, _P, _P], i),
         "siting_fbm_dem": ([_P, i, C.c_uint64, i, C.c_double, C.c_double, C.c_double,
@@ -331,6 +332,12 @@ class Context:
         cnt = C.c_int()
         self._check(self._lib.siting_last_pick_order(self.h, out.ctypes.data, cap, C.byref(cnt)))
         return out[:cnt.value]
+
+    def last_site_phase_cycles(self) -> list:
+        """Device cycles per SITE phase (CTA 0) of the last run."""
+        out = (C.c_longlong * 7)()
+        self._check(self._lib.siting_last_site_phase_cycles(self.h, out, 7))
+        return list(out)
 
     # ---- whole pipeline ---------------------------------------------------------
     def run(self, p: Params, elevs):

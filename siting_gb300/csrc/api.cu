@@ -209,8 +209,8 @@ int site_ctas_for(siting_ctx *ctx, int nsheds) {
 int site_enqueue(siting_ctx *ctx, int nrows, int roi, int intervis, int nsheds,
                  const int32_t *d_obs, const uint64_t *d_sheds, float bs, int nb, int npb,
                  uint8_t *d_selected, int *d_err) {
-  if (!ctx->h_out) CK(cudaMallocHost(&ctx->h_out, 8 * sizeof(long long)));
-  memset(ctx->h_out, 0, 8 * sizeof(long long));
+  if (!ctx->h_out) CK(cudaMallocHost(&ctx->h_out, 16 * sizeof(long long)));
+  memset(ctx->h_out, 0, 16 * sizeof(long long));
   if (nsheds <= 0) return SITING_OK;
   const int G = site_ctas_for(ctx, nsheds);
   if (!site_supported(roi, nsheds, G))
@@ -228,7 +228,7 @@ int site_enqueue(siting_ctx *ctx, int nrows, int roi, int intervis, int nsheds,
   CK(cudaMemsetAsync(d_selected, 0, nsheds, ctx->stream));
   CK(launch_site(nrows, roi, intervis, nsheds, d_obs, d_sheds, bs, nb, npb, d_selected, s, G,
                  d_err, ctx->stream));
-  CK(cudaMemcpyAsync(ctx->h_out, s.out, 3 * sizeof(long long), cudaMemcpyDeviceToHost,
+  CK(cudaMemcpyAsync(ctx->h_out, s.out, 10 * sizeof(long long), cudaMemcpyDeviceToHost,
                      ctx->stream));
   ctx->d_last_order = s.order;
   return SITING_OK;
@@ -580,6 +580,12 @@ int siting_last_pick_order(siting_ctx *ctx, int32_t *order, int cap, int *count)
                        ctx->stream));
     CK(cudaStreamSynchronize(ctx->stream));
   }
+  return SITING_OK;
+}
+
+int siting_last_site_phase_cycles(siting_ctx *ctx, long long *cycles, int n) {
+  if (!ctx || !cycles || n < 0) return SITING_EINVAL;
+  for (int i = 0; i < n && i < 7; i++) cycles[i] = ctx->h_out ? ctx->h_out[3 + i] : 0;
   return SITING_OK;
 }
 

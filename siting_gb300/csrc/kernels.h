@@ -72,7 +72,7 @@ struct SiteScratch {
   uint64_t *cum[2];   // nrows * ceil(nrows/64) words each, zeroed before launch
   uint64_t *slots;    // 2 * nctas * 2 words: {key, pos} per CTA per parity
   unsigned *bar;      // 2 words, zeroed
-  long long *out;     // [0] nused, [1] cumarea, [2] rounds
+  long long *out;     // [0] nused, [1] cumarea, [2] rounds, [3..9] phase cycles
   int32_t *order;     // nsheds: picks in order
 };
 size_t site_scratch_bytes(int nrows, int nsheds, int nctas);

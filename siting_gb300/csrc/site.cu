@@ -132,6 +132,16 @@ __global__ void __launch_bounds__(kSiteThreads, 1) site_kernel(const SiteArgs a)
   unsigned char *s_dirty = p;
 
   GroupBarrier gb{a.bar, (unsigned)G, 0u};
+  // tracing: device cycles per phase, accumulated by CTA 0's thread 0
+  long long ph[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+  long long tmark = clock64();
+  auto mark = [&](int i) {
+    if (k == 0 && tid == 0) {
+      const long long now = clock64();
+      ph[i] += now - tmark;
+      tmark = now;
+    }
+  };
 
   // ---- round 1 scores: popcount of every owned shed -----------------------
   for (int s = warp; s < my_slots; s += nwarps) {
@@ -164,6 +174,7 @@ __global__ void __launch_bounds__(kSiteThreads, 1) site_kernel(const SiteArgs a)
   }
   for (int g = tid; g < ngroups; g += blockDim.x) s_dirty[g] = 1;
   __syncthreads();
+  mark(0);
 
   long long cumarea = 0;
   int npicks = 0, t = 0;
@@ -232,7 +243,9 @@ __global__ void __launch_bounds__(kSiteThreads, 1) site_kernel(const SiteArgs a)
         }
       }
     }
+    mark(1);
     if (!group_sync(gb, a.err, &s_flag)) return;
+    mark(2);
     if (npicks > 0) {
       uint64_t *tmp = X;
       X = Y;
@@ -283,6 +296,7 @@ __global__ void __launch_bounds__(kSiteThreads, 1) site_kernel(const SiteArgs a)
       }
       __syncthreads();
     }
+    mark(3);
     const unsigned long long bkey = s_bestkey;
     const int area = (int)(bkey >> 32);
     if (area <= 0) break;
@@ -354,6 +368,7 @@ __global__ void __launch_bounds__(kSiteThreads, 1) site_kernel(const SiteArgs a)
       }
     }
     __syncthreads();
+    mark(4);
     if (tid == 0 && s_ncount != area) atomicOr(a.err, kErrSiteMismatch);
     const int nlist = min(s_nlist, a.list_cap);
 
@@ -377,6 +392,7 @@ __global__ void __launch_bounds__(kSiteThreads, 1) site_kernel(const SiteArgs a)
       if (d) atomicAdd(&s_delta[li], d);
     }
     __syncthreads();
+    mark(5);
 
     // ---- 4. new gains, intervis gate, dirty groups --------------------------
     for (int li = tid; li < nlist; li += blockDim.x) {
@@ -397,12 +413,14 @@ __global__ void __launch_bounds__(kSiteThreads, 1) site_kernel(const SiteArgs a)
       s_dirty[s >> 5] = 1;
     }
     __syncthreads();
+    mark(6);
   }
 
   if (k == 0 && tid == 0) {
     a.out[0] = npicks;
     a.out[1] = cumarea;
     a.out[2] = t;
+    for (int i = 0; i < 7; i++) a.out[3 + i] = ph[i];
   }
 }
 
