@@ -158,6 +158,8 @@ def run_gpu(args, w):
     g = sg.block_geometry(n, w["bw"], w["nwanted0"])
     dem = make_dem(w, seed_offset=rank)
     ctx = sg.Context(local)
+    if args.site_ctas:
+        ctx.set_site_ctas(args.site_ctas)
     stream = torch.cuda.ExternalStream(ctx.stream)
 
     # device-resident buffers
@@ -232,7 +234,7 @@ def run_gpu(args, w):
         "e2e": {"value": world * n * n / (mean_e2e / 1e3), "unit": "cells/s",
                 "ms_per_step": mean_e2e, "h2d_bytes_per_step": n * n * 2,
                 "d2h_bytes_per_step": g.nwanted * 5},
-        "gpu_launches": 4 * args.steps,
+        "gpu_launches": 5 * args.steps,
         "observers_per_s": world * g.nwanted / (mean_dev / 1e3),
         "stages_ms": {"vix": r.ms_vix, "findmax": r.ms_findmax, "viewshed": r.ms_viewshed,
                       "site": r.ms_site},
@@ -299,6 +301,8 @@ def main():
     ap.add_argument("--workload", default="c2_4096", choices=sorted(WORKLOADS))
     ap.add_argument("--cpu-sample-rows", type=int, default=2048)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--site-ctas", type=int, default=0,
+                    help="CTAs of the SITE kernel (0 = library default)")
     args = ap.parse_args()
     w = WORKLOADS[args.workload]
     rank = int(os.environ.get("RANK", "0"))

@@ -74,6 +74,7 @@ struct SiteScratch {
   unsigned *bar;      // 2 words, zeroed
   long long *out;     // [0] nused, [1] cumarea, [2] rounds, [3..9] phase cycles
   int32_t *order;     // nsheds: picks in order
+  int32_t *gains;     // nsheds: round-1 gains (site_score_kernel)
 };
 size_t site_scratch_bytes(int nrows, int nsheds, int nctas);
 void site_carve_scratch(void *base, int nrows, int nsheds, int nctas, SiteScratch *s);

@@ -53,6 +53,7 @@ struct SiteArgs {
   long long *out;
   int32_t *order;
   uint8_t *selected;
+  const int *gains;  // round-1 gains, from site_score_kernel
   int *err;
   int nslots, list_cap;
 };
@@ -94,6 +95,31 @@ __device__ __forceinline__ KeyPos warp_argmax(KeyPos v) {
   return v;
 }
 
+// Round 1 (siting.cpp:537-549 with nusedsheds == 0): the gain of every
+// candidate against an empty coverage is the popcount of its shed.  One warp
+// per shed, 128-bit loads, grid-stride: a pure HBM stream over all sheds.
+__global__ void __launch_bounds__(256) site_score_kernel(const uint64_t *sheds, int nsheds,
+                                                         int per, int *gains) {
+  const int lane = threadIdx.x & 31;
+  const int warps = gridDim.x * (blockDim.x >> 5);
+  for (int c = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; c < nsheds; c += warps) {
+    const uint64_t *sh = sheds + (size_t)c * per;
+    int cnt = 0;
+    if ((per & 1) == 0) {
+      const ulonglong2 *v = reinterpret_cast<const ulonglong2 *>(sh);
+      for (int i = lane; i < per / 2; i += 32) {
+        const ulonglong2 q = __ldg(v + i);
+        cnt += __popcll(q.x) + __popcll(q.y);
+      }
+    } else {
+      for (int i = lane; i < per; i += 32) cnt += __popcll(__ldg(sh + i));
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) cnt += __shfl_xor_sync(0xffffffffu, cnt, o);
+    if (lane == 0) gains[c] = cnt;
+  }
+}
+
 __global__ void __launch_bounds__(kSiteThreads, 1) site_kernel(const SiteArgs a) {
   extern __shared__ __align__(16) unsigned char sm[];
   __shared__ unsigned long long s_rkey[32];
@@ -127,6 +153,8 @@ __global__ void __launch_bounds__(kSiteThreads, 1) site_kernel(const SiteArgs a)
   p += (size_t)a.list_cap * 4;
   int *s_delta = reinterpret_cast<int *>(p);
   p += (size_t)a.list_cap * 4;
+  unsigned char *s_cov = p;
+  p += a.list_cap;
   unsigned char *s_used = p;
   p += a.nslots;
   unsigned char *s_dirty = p;
@@ -143,45 +171,31 @@ __global__ void __launch_bounds__(kSiteThreads, 1) site_kernel(const SiteArgs a)
     }
   };
 
-  // ---- round 1 scores: popcount of every owned shed -----------------------
-  for (int s = warp; s < my_slots; s += nwarps) {
-    const int c = s * G + k;
-    const uint64_t *sh = a.sheds + (size_t)c * per;
-    int cnt = 0;
-    if ((per & 1) == 0) {
-      const ulonglong2 *v = reinterpret_cast<const ulonglong2 *>(sh);
-      for (int i = lane; i < (int)(per / 2); i += 32) {
-        const ulonglong2 q = __ldg(v + i);
-        cnt += __popcll(q.x) + __popcll(q.y);
-      }
-    } else {
-      for (int i = lane; i < (int)per; i += 32) cnt += __popcll(__ldg(sh + i));
-    }
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) cnt += __shfl_xor_sync(0xffffffffu, cnt, o);
-    if (lane == 0) {
-      s_gain[s] = cnt;
-      s_area[s] = cnt;
+  // ---- own candidates: round-1 gains from the scoring kernel ----------------
+  for (int s = tid; s < a.nslots; s += blockDim.x) {
+    if (s < my_slots) {
+      const int c = s * G + k;
+      const int g = __ldcg(a.gains + c);
+      s_gain[s] = g;
+      s_area[s] = g;
       s_pos[s] = __ldg(a.obs + c);
       s_used[s] = 0;
+    } else {
+      s_gain[s] = 0;
+      s_area[s] = 0;
+      s_pos[s] = 0;
+      s_used[s] = 1;
     }
-  }
-  for (int s = my_slots + tid; s < a.nslots; s += blockDim.x) {
-    s_gain[s] = 0;
-    s_area[s] = 0;
-    s_pos[s] = 0;
-    s_used[s] = 1;
   }
   for (int g = tid; g < ngroups; g += blockDim.x) s_dirty[g] = 1;
   __syncthreads();
   mark(0);
 
   long long cumarea = 0;
-  int npicks = 0, t = 0;
+  int npicks = 0;
   uint64_t *X = a.cum0, *Y = a.cum1;
   uint64_t *ncur = nbuf0, *nprev = nbuf1;
-  int prev_px = 0, prev_fw = 0;
-  bool have_prev = false;
+  int prev_px = 0, prev_fw = 0, cur_px = 0, cur_fw = 0;
   const double ncells = (double)n * (double)n;
 
   for (;;) {
@@ -216,86 +230,55 @@ __global__ void __launch_bounds__(kSiteThreads, 1) site_kernel(const SiteArgs a)
           const int c = (int)(0xFFFFFFFFu - (unsigned)(key & 0xFFFFFFFFull));
           pos = s_pos[c / G];
         }
-        unsigned long long *slot = a.slots + ((size_t)(t & 1) * G + k) * 2;
+        unsigned long long *slot = a.slots + ((size_t)(npicks & 1) * G + k) * 2;
         __stcg(slot, key);
         __stcg(slot + 1, (unsigned long long)pos);
-      }
-    }
-    // CTA 0: bring the coverage buffer that is read next round up to date.
-    if (k == 0 && npicks > 0) {
-      const int px = s_bestpos / n;  // pick of the round just finished
-      int fw, fb;
-      shed_align(s_bestpos - px * n - roi, fw, fb);
-      (void)fb;
-      for (int i = tid; i < nr * nbw; i += blockDim.x) {
-        const int prow = i / nbw, j = i - prow * nbw;
-        uint64_t v = ncur[i];
-        int gr = px - roi + prow, W = fw + j;
-        // the two windows overlap when the picks are within 2*roi: OR atomically
-        if (v && gr >= 0 && gr < n && W >= 0 && W < cw)
-          atomicOr(reinterpret_cast<unsigned long long *>(Y + (size_t)gr * cw + W), v);
-        if (have_prev) {
-          v = nprev[i];
-          gr = prev_px - roi + prow;
-          W = prev_fw + j;
-          if (v && gr >= 0 && gr < n && W >= 0 && W < cw)
-            atomicOr(reinterpret_cast<unsigned long long *>(Y + (size_t)gr * cw + W), v);
-        }
       }
     }
     mark(1);
     if (!group_sync(gb, a.err, &s_flag)) return;
     mark(2);
-    if (npicks > 0) {
+    if (npicks > 0) {  // the buffer written last round is complete: read it now
       uint64_t *tmp = X;
       X = Y;
       Y = tmp;
-      if (k == 0) {
-        const int px = s_bestpos / n;
-        int fw, fb;
-        shed_align(s_bestpos - px * n - roi, fw, fb);
-        (void)fb;
-        prev_px = px;
-        prev_fw = fw;
-        have_prev = true;
-        uint64_t *tb = ncur;
-        ncur = nprev;
-        nprev = tb;
-      }
+      uint64_t *tb = ncur;
+      ncur = nprev;
+      nprev = tb;
+      prev_px = cur_px;
+      prev_fw = cur_fw;
     }
 
     // ---- 1. agree on the pick ---------------------------------------------
-    {
+    if (warp * 32 < G) {
       KeyPos v{0ull, 0};
       if (tid < G) {
-        const unsigned long long *slot = a.slots + ((size_t)(t & 1) * G + tid) * 2;
+        const unsigned long long *slot = a.slots + ((size_t)(npicks & 1) * G + tid) * 2;
         v.key = __ldcg(slot);
         v.pos = (int)__ldcg(slot + 1);
       }
-      if (warp * 32 < G) {
-        v = warp_argmax(v);
-        if (lane == 0) {
-          s_rkey[warp] = v.key;
-          s_rpos[warp] = v.pos;
-        }
+      v = warp_argmax(v);
+      if (lane == 0) {
+        s_rkey[warp] = v.key;
+        s_rpos[warp] = v.pos;
       }
-      __syncthreads();
-      if (warp == 0) {
-        KeyPos w{0ull, 0};
-        if (lane * 32 < G) {
-          w.key = s_rkey[lane];
-          w.pos = s_rpos[lane];
-        }
-        w = warp_argmax(w);
-        if (lane == 0) {
-          s_bestkey = w.key;
-          s_bestpos = w.pos;
-          s_nlist = 0;
-          s_ncount = 0;
-        }
-      }
-      __syncthreads();
     }
+    if (G > 32) __syncthreads();
+    if (warp == 0) {
+      KeyPos w{0ull, 0};
+      if (lane * 32 < G) {
+        w.key = s_rkey[lane];
+        w.pos = s_rpos[lane];
+      }
+      w = warp_argmax(w);
+      if (lane == 0) {
+        s_bestkey = w.key;
+        s_bestpos = w.pos;
+        s_nlist = 0;
+        s_ncount = 0;
+      }
+    }
+    __syncthreads();
     mark(3);
     const unsigned long long bkey = s_bestkey;
     const int area = (int)(bkey >> 32);
@@ -313,13 +296,14 @@ __global__ void __launch_bounds__(kSiteThreads, 1) site_kernel(const SiteArgs a)
       if (k == 0) a.order[npicks] = pc;
     }
     npicks++;
-    t++;
     if (100.0 * (double)cumarea / ncells > 95.0) break;
 
     // ---- 2. newly covered bits of the pick --------------------------------
     const int px = bpos / n, py = bpos - (bpos / n) * n;
     int fwp, fbp;
     shed_align(py - roi, fwp, fbp);
+    cur_px = px;
+    cur_fw = fwp;
     {
       const uint64_t *shp = a.sheds + (size_t)pc * per;
       int cnt = 0;
@@ -340,10 +324,10 @@ __global__ void __launch_bounds__(kSiteThreads, 1) site_kernel(const SiteArgs a)
     // ---- 3a. own unused candidates within 2*roi of the pick ---------------
     {
       const float r2f = (float)(2 * roi);
-      const int bxl = max(0, (int)floorf(((float)px - r2f) / a.bs) - 1);
-      const int bxh = min(a.nb - 1, (int)floorf(((float)px + r2f) / a.bs) + 1);
-      const int byl = max(0, (int)floorf(((float)py - r2f) / a.bs) - 1);
-      const int byh = min(a.nb - 1, (int)floorf(((float)py + r2f) / a.bs) + 1);
+      const int bxl = max(0, (int)floorf(((float)px - r2f) / a.bs) - 2);
+      const int bxh = min(a.nb - 1, (int)floorf(((float)px + r2f) / a.bs) + 2);
+      const int byl = max(0, (int)floorf(((float)py - r2f) / a.bs) - 2);
+      const int byh = min(a.nb - 1, (int)floorf(((float)py + r2f) / a.bs) + 2);
       const int run = (byh - byl + 1) * a.npb;  // contiguous indices per block row
       const int per_run = run / G + 2;
       const int items = (bxh - bxl + 1) * per_run;
@@ -362,6 +346,7 @@ __global__ void __launch_bounds__(kSiteThreads, 1) site_kernel(const SiteArgs a)
         if (idx < a.list_cap) {
           s_list[idx] = s;
           s_delta[idx] = 0;
+          s_cov[idx] = 0;
         } else {
           atomicOr(a.err, kErrCapacity);
         }
@@ -372,13 +357,38 @@ __global__ void __launch_bounds__(kSiteThreads, 1) site_kernel(const SiteArgs a)
     if (tid == 0 && s_ncount != area) atomicOr(a.err, kErrSiteMismatch);
     const int nlist = min(s_nlist, a.list_cap);
 
-    // ---- 3b. subtract the overlap with N ----------------------------------
+    // ---- coverage buffer for next round: this CTA's rows of N_t and N_{t-1}
+    for (int i = tid; i < nr * nbw; i += blockDim.x) {
+      const int prow = i / nbw;
+      if (prow % G != k) continue;
+      const int j = i - prow * nbw;
+      uint64_t v = ncur[i];
+      int gr = cur_px - roi + prow, W = cur_fw + j;
+      if (v && gr >= 0 && gr < n && W >= 0 && W < cw)
+        atomicOr(reinterpret_cast<unsigned long long *>(Y + (size_t)gr * cw + W), v);
+      if (npicks > 1) {
+        v = nprev[i];
+        gr = prev_px - roi + prow;
+        W = prev_fw + j;
+        if (v && gr >= 0 && gr < n && W >= 0 && W < cw)
+          atomicOr(reinterpret_cast<unsigned long long *>(Y + (size_t)gr * cw + W), v);
+      }
+    }
+
+    // ---- 3b. subtract the overlap with N; coverage bit of own cell ----------
     for (int i = tid; i < nlist * nr; i += blockDim.x) {
       const int li = i / nr, r = i - li * nr;
       const int s = s_list[li];
       const int cp = s_pos[s];
       const int cx = cp / n, cy = cp - cx * n;
       const int gr = cx - roi + r, prow = gr - (px - roi);
+      if (a.intervis && r == roi) {  // the candidate's own cell: covered after p?
+        int cov = (int)((__ldcg(X + (size_t)cx * cw + (cy >> 6)) >> (63 - (cy & 63))) & 1ull);
+        const int j = (cy >> 6) - fwp;
+        if (!cov && prow >= 0 && prow < nr && j >= 0 && j < nbw)
+          cov = (int)((ncur[prow * nbw + j] >> (63 - (cy & 63))) & 1ull);
+        s_cov[li] = (unsigned char)cov;
+      }
       if (prow < 0 || prow >= nr || gr < 0 || gr >= n) continue;
       int fwc, fbc;
       shed_align(cy - roi, fwc, fbc);
@@ -386,9 +396,10 @@ __global__ void __launch_bounds__(kSiteThreads, 1) site_kernel(const SiteArgs a)
       const int lo = max(max(fwc, fwp), 0), hi = min(min(lwc, fwp + nwpr), cw - 1);
       if (lo > hi) continue;
       const uint64_t *row = a.sheds + (size_t)(s * G + k) * per + (size_t)r * nwpr;
-      const uint64_t *nrow = ncur + (size_t)prow * nbw - fwp;
+      const uint64_t *nrow = ncur + prow * nbw;
       int d = 0;
-      for (int W = lo; W <= hi; W++) d += __popcll(placed_word(row, W - fwc, nwpr, fbc) & nrow[W]);
+      for (int W = lo; W <= hi; W++)
+        d += __popcll(placed_word(row, W - fwc, nwpr, fbc) & nrow[W - fwp]);
       if (d) atomicAdd(&s_delta[li], d);
     }
     __syncthreads();
@@ -399,17 +410,7 @@ __global__ void __launch_bounds__(kSiteThreads, 1) site_kernel(const SiteArgs a)
       const int s = s_list[li];
       const int g = s_gain[s] - s_delta[li];
       s_gain[s] = g;
-      int ar = g;
-      if (a.intervis) {
-        const int cp = s_pos[s];
-        const int cx = cp / n, cy = cp - cx * n;
-        int cov = (int)((__ldcg(X + (size_t)cx * cw + (cy >> 6)) >> (63 - (cy & 63))) & 1ull);
-        const int prow = cx - (px - roi), j = (cy >> 6) - fwp;
-        if (!cov && prow >= 0 && prow < nr && j >= 0 && j < nbw)
-          cov = (int)((ncur[prow * nbw + j] >> (63 - (cy & 63))) & 1ull);
-        if (!cov) ar = 0;
-      }
-      s_area[s] = ar;
+      s_area[s] = (!a.intervis || s_cov[li]) ? g : 0;
       s_dirty[s >> 5] = 1;
     }
     __syncthreads();
@@ -419,7 +420,7 @@ __global__ void __launch_bounds__(kSiteThreads, 1) site_kernel(const SiteArgs a)
   if (k == 0 && tid == 0) {
     a.out[0] = npicks;
     a.out[1] = cumarea;
-    a.out[2] = t;
+    a.out[2] = npicks;
     for (int i = 0; i < 7; i++) a.out[3 + i] = ph[i];
   }
 }
@@ -444,7 +445,7 @@ size_t site_scratch_bytes(int nrows, int nsheds, int nctas) {
   size_t b = 2 * (size_t)nrows * cw * 8;
   b += (size_t)2 * nctas * 2 * 8;
   b += 256;  // barrier + out
-  b += ((size_t)nsheds * 4 + 255) & ~(size_t)255;
+  b += 2 * (((size_t)nsheds * 4 + 255) & ~(size_t)255);  // order + gains
   return b + 1024;
 }
 
@@ -462,11 +463,14 @@ void site_carve_scratch(void *base, int nrows, int nsheds, int nctas, SiteScratc
   s->bar = reinterpret_cast<unsigned *>(take(64));
   s->out = reinterpret_cast<long long *>(take(64));
   s->order = reinterpret_cast<int32_t *>(take((size_t)nsheds * 4));
+  s->gains = reinterpret_cast<int32_t *>(take((size_t)nsheds * 4));
 }
 
+// Few CTAs keep the per-round barrier and the redundant reads of the pick's
+// shed cheap; enough CTAs keep each one's candidates within kMaxSlots.
 int site_default_ctas(int nsheds, int sm_count) {
-  int g = std::max(1, (nsheds + 255) / 256);
-  g = std::max(g, (nsheds + kMaxSlots - 1) / kMaxSlots);
+  int g = std::max(32, (nsheds + kMaxSlots - 1) / kMaxSlots);
+  g = std::min(g, std::max(1, nsheds));
   return std::min(g, sm_count);
 }
 
@@ -478,7 +482,7 @@ size_t site_smem_bytes(int roi, int nsheds, int nctas, int nblocks, int npb, flo
   size_t b = 2 * (size_t)nr * nbw * 8;
   b += (size_t)ngroups * 8;
   b += (size_t)nslots * 12;
-  b += (size_t)cap * 8;
+  b += (size_t)cap * 9;
   b += nslots + ngroups;
   return (b + 15) & ~(size_t)15;
 }
@@ -510,12 +514,20 @@ cudaError_t launch_site(int nrows, int roi, int intervis, int nsheds, const int3
   a.out = s.out;
   a.order = s.order;
   a.selected = selected;
+  a.gains = s.gains;
   a.err = d_err;
   a.nslots = (nsheds + nctas - 1) / nctas;
   a.list_cap = site_list_cap(roi, nsheds, nctas, nblocks, npb, blocksize);
   const size_t shm = site_smem_bytes(roi, nsheds, nctas, nblocks, npb, blocksize);
-  cudaError_t e =
-      cudaFuncSetAttribute(site_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shm);
+  const int nr = 2 * roi + 1, per = nr * ((nr + 63) / 64);
+  int dev = 0, sms = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  const int sgrid = std::max(1, std::min(sms * 8, (nsheds + 7) / 8));
+  site_score_kernel<<<sgrid, 256, 0, st>>>(sheds, nsheds, per, s.gains);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+  e = cudaFuncSetAttribute(site_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shm);
   if (e != cudaSuccess) return e;
   void *args[] = {&a};
   return cudaLaunchCooperativeKernel((void *)site_kernel, dim3(nctas), dim3(kSiteThreads), args,

@@ -19,6 +19,8 @@
 //
 // Bit-exactness: separately rounded FP32 operations, IEEE division for the
 // slopes, round-half-away-from-zero for the minor coordinate.
+#include <algorithm>
+
 #include "common.cuh"
 #include "kernels.h"
 
@@ -102,7 +104,7 @@ __device__ __forceinline__ void sweep_rays(const Dem &dem, const ShedArgs &a, in
 }
 
 template <bool kSmem>
-__global__ void __launch_bounds__(256) shed_kernel(const __grid_constant__ CUtensorMap map,
+__global__ void __launch_bounds__(1024) shed_kernel(const __grid_constant__ CUtensorMap map,
                                                    const ShedArgs a) {
   extern __shared__ __align__(128) unsigned char sm[];
   const int nr = 2 * a.roi + 1, nwpr = (nr + 63) / 64, nwords = nr * nwpr;
@@ -171,7 +173,11 @@ size_t shed_smem_bytes(const ShedPlan &p, int roi) {
 }
 
 ShedPlan shed_default_plan(int roi) {
-  ShedPlan p{256, true};
+  // one ray per thread where 8*roi rays fit a CTA, else an even split
+  const int rays = 8 * roi;
+  const int rounds = (rays + 1023) / 1024;
+  const int threads = std::min(1024, ((rays + rounds - 1) / rounds + 31) / 32 * 32);
+  ShedPlan p{std::max(threads, 64), true};
   const WinGeom g = win_geom(roi);
   if (g.w > 256 || shed_smem_bytes(p, roi) > 110 * 1024) p.use_smem = false;
   return p;

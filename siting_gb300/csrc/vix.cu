@@ -76,14 +76,19 @@ __device__ __forceinline__ int vix_target(const Dem &dem, int n, int roi, int ro
   const float drecip = d > 0 ? rr : -rr;
   const float slope = fmul(i2f(m), drecip);
   const float zslope = fmul(i2f(tz - oz), drecip);
-  const int sg = d > 0 ? 1 : -1;
+  // Sample offsets are +-1, 2, 4, ...: scaling by a power of two is exact in
+  // FP32, so slope*id and id*zslope are carried by doubling, bit-identical to
+  // the reference's products.
+  float sl = d > 0 ? slope : -slope;
+  float zs = d > 0 ? zslope : -zslope;
+  const int sx = mx ? (d > 0 ? 1 : -1) : 0, sy = mx ? 0 : (d > 0 ? 1 : -1);
   for (int step = 1; step < ad; step <<= 1) {
-    const int id = sg * step;
-    const float fid = i2f(id);
-    const int off = round_i(fmul(slope, fid));
-    const int x = mx ? ox + id : ox + off;
-    const int y = mx ? oy + off : oy + id;
-    if (i2f(dem.at(x, y)) > fadd(foz, fmul(fid, zslope))) return 0;
+    const int off = round_i(sl);
+    const int x = mx ? ox + sx * step : ox + off;
+    const int y = mx ? oy + off : oy + sy * step;
+    if (i2f(dem.at(x, y)) > fadd(foz, zs)) return 0;
+    sl = fadd(sl, sl);
+    zs = fadd(zs, zs);
   }
   return 1;
 }
@@ -131,7 +136,7 @@ __device__ __forceinline__ void vix_tile_work(const Dem &dem, const VixArgs &a, 
 }
 
 template <bool kSmem>
-__global__ void __launch_bounds__(512) vix_kernel(const __grid_constant__ CUtensorMap map,
+__global__ void __launch_bounds__(1024) vix_kernel(const __grid_constant__ CUtensorMap map,
                                                   const VixArgs a) {
   extern __shared__ __align__(128) unsigned char sm[];
   const int T = a.tile;
@@ -241,10 +246,10 @@ size_t vix_smem_bytes(const VixPlan &p, int roi, int ntests) {
 
 VixPlan vix_default_plan(int nrows, int roi, int ntests) {
   (void)nrows;
-  VixPlan p{32, 512, false};
+  VixPlan p{32, 1024, false};
   const size_t limit = 220 * 1024;
   for (int tile : {64, 32, 16}) {
-    VixPlan q{tile, 512, true};
+    VixPlan q{tile, 1024, true};
     const HaloGeom g = halo_geom(tile, roi);
     if (g.w <= 256 && vix_smem_bytes(q, roi, ntests) <= limit) return q;
   }
