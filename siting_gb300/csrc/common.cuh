@@ -86,38 +86,35 @@ __device__ __forceinline__ void tma_load_2d(void *dst, const CUtensorMap *map, i
 }
 
 // ---- bounded barrier over a group of co-resident CTAs ------------------------
-// bar[0] = arrival count, bar[1] = generation.  Must be reached by all
-// threads of every CTA of the group.  Returns false (and sets err) when the
-// wait expired; the group then abandons its work.
+// bar[0] counts arrivals and is never reset: the g-th barrier completes when
+// it reaches g * nctas.  One release-add per CTA, then acquire-polls.  Must be
+// reached by all threads of every CTA of the group.  Returns false (and sets
+// err) when the wait expired; the group then abandons its work.
 struct GroupBarrier {
   unsigned *bar;
   unsigned nctas;
   unsigned gen;
 };
 
+__device__ __forceinline__ void red_release_add(unsigned *p, unsigned v) {
+  asm volatile("red.release.gpu.global.add.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+
 __device__ __forceinline__ bool group_sync(GroupBarrier &b, int *err, int *s_flag) {
   __syncthreads();
+  b.gen++;
   if (threadIdx.x == 0) {
     int ok = 1;
-    __threadfence();
-    const unsigned g = b.gen;
-    const unsigned arrived = atomicAdd(&b.bar[0], 1u);
-    if (arrived == b.nctas - 1) {
-      atomicExch(&b.bar[0], 0u);
-      __threadfence();
-      st_release_u32(&b.bar[1], g + 1);
-    } else {
-      const long long t0 = clock64();
-      while (ld_acquire_u32(&b.bar[1]) == g) {
-        if (clock64() - t0 > kWaitCycles) {
-          atomicOr(err, kErrBarrierTimeout);
-          ok = 0;
-          break;
-        }
+    red_release_add(&b.bar[0], 1u);
+    const unsigned target = b.gen * b.nctas;
+    const long long t0 = clock64();
+    while ((int)(ld_acquire_u32(&b.bar[0]) - target) < 0) {
+      if (clock64() - t0 > kWaitCycles) {
+        atomicOr(err, kErrBarrierTimeout);
+        ok = 0;
+        break;
       }
     }
-    b.gen = g + 1;
-    __threadfence();
     *s_flag = ok;
   }
   __syncthreads();

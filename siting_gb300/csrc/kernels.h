@@ -79,6 +79,8 @@ struct SiteScratch {
 size_t site_scratch_bytes(int nrows, int nsheds, int nctas);
 void site_carve_scratch(void *base, int nrows, int nsheds, int nctas, SiteScratch *s);
 int site_default_ctas(int nsheds, int sm_count);
+// Smallest covered-cell count at which the reference's 95% stop test holds.
+long long site_stop_area(int nrows);
 size_t site_smem_bytes(int roi, int nsheds, int nctas, int nblocks, int npb, float blocksize);
 bool site_supported(int roi, int nsheds, int nctas);
 cudaError_t launch_site(int nrows, int roi, int intervis, int nsheds, const int32_t *obs,

@@ -56,6 +56,7 @@ struct SiteArgs {
   const int *gains;  // round-1 gains, from site_score_kernel
   int *err;
   int nslots, list_cap;
+  long long stop_area;  // smallest cumarea with 100.0*cumarea/n^2 > 95 (host-computed)
 };
 
 __device__ __forceinline__ void shed_align(int c0, int &fw, int &fb) {
@@ -196,7 +197,6 @@ __global__ void __launch_bounds__(kSiteThreads, 1) site_kernel(const SiteArgs a)
   uint64_t *X = a.cum0, *Y = a.cum1;
   uint64_t *ncur = nbuf0, *nprev = nbuf1;
   int prev_px = 0, prev_fw = 0, cur_px = 0, cur_fw = 0;
-  const double ncells = (double)n * (double)n;
 
   for (;;) {
     // ---- refresh dirty groups and publish this CTA's maximum --------------
@@ -296,7 +296,7 @@ __global__ void __launch_bounds__(kSiteThreads, 1) site_kernel(const SiteArgs a)
       if (k == 0) a.order[npicks] = pc;
     }
     npicks++;
-    if (100.0 * (double)cumarea / ncells > 95.0) break;
+    if (cumarea >= a.stop_area) break;  // 100.0*cumarea/n^2 > 95 (siting.cpp:602-604)
 
     // ---- 2. newly covered bits of the pick --------------------------------
     const int px = bpos / n, py = bpos - (bpos / n) * n;
@@ -440,6 +440,24 @@ int site_list_cap(int roi, int nsheds, int G, int nb, int npb, float bs) {
 
 }  // namespace
 
+// The reference stops once 100.0 * cumarea / square(nrows) > 95, evaluated in
+// double (siting.cpp:602-604).  The expression is non-decreasing in cumarea,
+// so the first cumarea where it holds is found once, on the host, with the
+// same double arithmetic; the kernel then compares integers.
+long long site_stop_area(int nrows) {
+  const int sq = nrows * nrows;
+  auto over = [&](long long c) { return 100.0 * (int)c / sq > 95; };
+  long long lo = 0, hi = (long long)sq + 1;  // over(hi) is true
+  while (lo < hi) {
+    const long long mid = lo + (hi - lo) / 2;
+    if (over(mid))
+      hi = mid;
+    else
+      lo = mid + 1;
+  }
+  return lo;
+}
+
 size_t site_scratch_bytes(int nrows, int nsheds, int nctas) {
   const size_t cw = (size_t)(nrows + 63) / 64;
   size_t b = 2 * (size_t)nrows * cw * 8;
@@ -518,6 +536,7 @@ cudaError_t launch_site(int nrows, int roi, int intervis, int nsheds, const int3
   a.err = d_err;
   a.nslots = (nsheds + nctas - 1) / nctas;
   a.list_cap = site_list_cap(roi, nsheds, nctas, nblocks, npb, blocksize);
+  a.stop_area = site_stop_area(nrows);
   const size_t shm = site_smem_bytes(roi, nsheds, nctas, nblocks, npb, blocksize);
   const int nr = 2 * roi + 1, per = nr * ((nr + 63) / 64);
   int dev = 0, sms = 0;
