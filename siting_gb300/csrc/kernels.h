@@ -69,12 +69,14 @@ cudaError_t launch_sheds(const DemView &dem, int roi, int oht, int tht, int nshe
 // ---- SITE -----------------------------------------------------------------------
 // Scratch layout of one SITE job (device, carved from one allocation).
 struct SiteScratch {
-  uint64_t *cum[2];   // nrows * ceil(nrows/64) words each, zeroed before launch
-  uint64_t *slots;    // 2 * nctas * 2 words: {key, pos} per CTA per parity
-  unsigned *bar;      // 2 words, zeroed
-  long long *out;     // [0] nused, [1] cumarea, [2] rounds, [3..9] phase cycles
-  int32_t *order;     // nsheds: picks in order
-  int32_t *gains;     // nsheds: round-1 gains (site_score_kernel)
+  uint64_t *cum[2];          // nrows * ceil(nrows/64) words each, zeroed before launch
+  unsigned long long *topk;  // [2][nctas][8] x {key, cell}: published top keys
+  int *cuts;                 // [2][nctas]: per-CTA prefix cut (intervis)
+  int *ncount;               // [2][64]: popcount of each pick's new bits (self-check)
+  unsigned *bar;             // group barrier counter, zeroed
+  long long *out;            // [0] nused, [1] cumarea, [2] rounds, [3..9] phase cycles
+  int32_t *order;            // nsheds: picks in order
+  int32_t *gains;            // nsheds: round-1 gains (site_score_kernel)
 };
 size_t site_scratch_bytes(int nrows, int nsheds, int nctas);
 void site_carve_scratch(void *base, int nrows, int nsheds, int nctas, SiteScratch *s);

@@ -40,6 +40,9 @@ namespace {
 
 constexpr int kSiteThreads = 1024;
 constexpr int kMaxSlots = 4096;  // candidates owned by one CTA
+constexpr int kTopK = 8;         // keys each CTA publishes per round
+constexpr int kMaxPicks = 64;    // picks accepted in one round at most
+constexpr int kMaxPairs = 8192;  // (candidate, pick) pairs one CTA updates per round
 
 struct SiteArgs {
   int n, roi, intervis, nsheds, G;
@@ -48,14 +51,16 @@ struct SiteArgs {
   float bs;
   int nb, npb;
   uint64_t *cum0, *cum1;
-  unsigned long long *slots;  // [2][G] x {key, cell}
+  unsigned long long *topk;  // [2][G][kTopK] x {key, cell}
+  int *cuts;                 // [2][G]: per-CTA cut of the round's prefix (intervis)
+  int *ncount;               // [2][kMaxPicks]: popcount of each pick's new bits
   unsigned *bar;
   long long *out;
   int32_t *order;
   uint8_t *selected;
   const int *gains;  // round-1 gains, from site_score_kernel
   int *err;
-  int nslots, list_cap;
+  int nslots, pick_items, pick_cap, pair_cap;
   long long stop_area;  // smallest cumarea with 100.0*cumarea/n^2 > 95 (host-computed)
 };
 
@@ -77,23 +82,25 @@ __device__ __forceinline__ uint64_t placed_word(const uint64_t *row, int j, int 
 __device__ __forceinline__ unsigned long long make_key(int area, int c) {
   return ((unsigned long long)(unsigned)area << 32) | (unsigned long long)(0xFFFFFFFFu - (unsigned)c);
 }
+__device__ __forceinline__ int key_index(unsigned long long key) {
+  return (int)(0xFFFFFFFFu - (unsigned)(key & 0xFFFFFFFFull));
+}
 
-struct KeyPos {
-  unsigned long long key;
-  int pos;
-};
+// Slot flags
+constexpr unsigned char kUsed = 1, kTaken = 2, kInel = 4;
 
-__device__ __forceinline__ KeyPos warp_argmax(KeyPos v) {
+__device__ __forceinline__ unsigned long long group_key(const int *s_area,
+                                                        const unsigned char *s_flag, int g,
+                                                        int lane, int my_slots, int G, int k) {
+  const int s = g * 32 + lane;
+  unsigned long long key = 0;
+  if (s < my_slots && !(s_flag[s] & (kUsed | kTaken))) key = make_key(s_area[s], s * G + k);
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) {
-    const unsigned long long k = __shfl_xor_sync(0xffffffffu, v.key, o);
-    const int p = __shfl_xor_sync(0xffffffffu, v.pos, o);
-    if (k > v.key) {
-      v.key = k;
-      v.pos = p;
-    }
+    const unsigned long long w = __shfl_xor_sync(0xffffffffu, key, o);
+    key = w > key ? w : key;
   }
-  return v;
+  return key;
 }
 
 // Round 1 (siting.cpp:537-549 with nusedsheds == 0): the gain of every
@@ -123,42 +130,44 @@ __global__ void __launch_bounds__(256) site_score_kernel(const uint64_t *sheds, 
 
 __global__ void __launch_bounds__(kSiteThreads, 1) site_kernel(const SiteArgs a) {
   extern __shared__ __align__(16) unsigned char sm[];
-  __shared__ unsigned long long s_rkey[32];
-  __shared__ int s_rpos[32];
-  __shared__ unsigned long long s_bestkey;
-  __shared__ int s_bestpos, s_nlist, s_flag, s_ncount;
+  __shared__ int s_m, s_mcut, s_stop_at, s_done, s_npair, s_flagv, s_roundcut;
+  __shared__ long long s_cum;
 
   const int G = a.G, k = blockIdx.x;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nwarps = blockDim.x >> 5;
-  const int n = a.n, roi = a.roi, nr = 2 * roi + 1, nwpr = (nr + 63) / 64, nbw = nwpr + 1;
+  const int n = a.n, roi = a.roi, nr = 2 * roi + 1, nwpr = (nr + 63) / 64;
   const int cw = (n + 63) / 64;
   const size_t per = (size_t)nr * nwpr;
   const int my_slots = k < a.nsheds ? (a.nsheds - k + G - 1) / G : 0;
   const int ngroups = (a.nslots + 31) / 32;
+  const int GK = G * kTopK;
 
   // shared-memory carve-up (sizes mirrored by site_smem_bytes)
   unsigned char *p = sm;
-  uint64_t *nbuf0 = reinterpret_cast<uint64_t *>(p);
-  p += (size_t)nr * nbw * 8;
-  uint64_t *nbuf1 = reinterpret_cast<uint64_t *>(p);
-  p += (size_t)nr * nbw * 8;
-  unsigned long long *s_gmax = reinterpret_cast<unsigned long long *>(p);
-  p += (size_t)ngroups * 8;
-  int *s_gain = reinterpret_cast<int *>(p);
-  p += (size_t)a.nslots * 4;
-  int *s_area = reinterpret_cast<int *>(p);
-  p += (size_t)a.nslots * 4;
-  int *s_pos = reinterpret_cast<int *>(p);
-  p += (size_t)a.nslots * 4;
-  int *s_list = reinterpret_cast<int *>(p);
-  p += (size_t)a.list_cap * 4;
-  int *s_delta = reinterpret_cast<int *>(p);
-  p += (size_t)a.list_cap * 4;
-  unsigned char *s_cov = p;
-  p += a.list_cap;
-  unsigned char *s_used = p;
-  p += a.nslots;
-  unsigned char *s_dirty = p;
+  auto take = [&](size_t bytes) {
+    unsigned char *q = p;
+    p += (bytes + 15) & ~(size_t)15;
+    return q;
+  };
+  unsigned long long *s_gmax = reinterpret_cast<unsigned long long *>(take((size_t)ngroups * 8));
+  unsigned long long *s_mkey = reinterpret_cast<unsigned long long *>(take((size_t)GK * 8));
+  unsigned long long *s_pkey = reinterpret_cast<unsigned long long *>(take(kMaxPicks * 8));
+  int *s_gain = reinterpret_cast<int *>(take((size_t)a.nslots * 4));
+  int *s_area = reinterpret_cast<int *>(take((size_t)a.nslots * 4));
+  int *s_pos = reinterpret_cast<int *>(take((size_t)a.nslots * 4));
+  int *s_dacc = reinterpret_cast<int *>(take((size_t)a.nslots * 4));
+  int *s_mpos = reinterpret_cast<int *>(take((size_t)GK * 4));
+  int *s_pk = reinterpret_cast<int *>(take(kMaxPicks * 4));    // pick: candidate index
+  int *s_ppos = reinterpret_cast<int *>(take(kMaxPicks * 4));  // pick: cell
+  int *s_prevpos = reinterpret_cast<int *>(take(kMaxPicks * 4));
+  int *s_prevpk = reinterpret_cast<int *>(take(kMaxPicks * 4));
+  int *s_pairslot = reinterpret_cast<int *>(take((size_t)a.pair_cap * 4));
+  int *s_pairdelta = reinterpret_cast<int *>(take((size_t)a.pair_cap * 4));
+  unsigned char *s_pairpick = take((size_t)a.pair_cap);
+  unsigned char *s_paircov = take((size_t)a.pair_cap);
+  unsigned char *s_flag = take((size_t)a.nslots);
+  unsigned char *s_tag = take((size_t)a.nslots);  // bit0 touched, bit1 covered (this round)
+  unsigned char *s_dirty = take((size_t)ngroups);
 
   GroupBarrier gb{a.bar, (unsigned)G, 0u};
   // tracing: device cycles per phase, accumulated by CTA 0's thread 0
@@ -174,42 +183,34 @@ __global__ void __launch_bounds__(kSiteThreads, 1) site_kernel(const SiteArgs a)
 
   // ---- own candidates: round-1 gains from the scoring kernel ----------------
   for (int s = tid; s < a.nslots; s += blockDim.x) {
-    if (s < my_slots) {
-      const int c = s * G + k;
-      const int g = __ldcg(a.gains + c);
-      s_gain[s] = g;
-      s_area[s] = g;
-      s_pos[s] = __ldg(a.obs + c);
-      s_used[s] = 0;
-    } else {
-      s_gain[s] = 0;
-      s_area[s] = 0;
-      s_pos[s] = 0;
-      s_used[s] = 1;
-    }
+    const bool mine = s < my_slots;
+    const int c = s * G + k;
+    const int g = mine ? __ldcg(a.gains + c) : 0;
+    s_gain[s] = g;
+    s_area[s] = g;
+    s_pos[s] = mine ? __ldg(a.obs + c) : 0;
+    s_flag[s] = mine ? 0 : kUsed;
+    s_dacc[s] = 0;
+    s_tag[s] = 0;
   }
   for (int g = tid; g < ngroups; g += blockDim.x) s_dirty[g] = 1;
+  if (tid == 0) {
+    s_cum = 0;
+    s_done = 0;
+  }
   __syncthreads();
   mark(0);
 
-  long long cumarea = 0;
-  int npicks = 0;
   uint64_t *X = a.cum0, *Y = a.cum1;
-  uint64_t *ncur = nbuf0, *nprev = nbuf1;
-  int prev_px = 0, prev_fw = 0, cur_px = 0, cur_fw = 0;
+  int npicks = 0, rounds = 0, nprev = 0;
+  const int lim2 = 4 * roi * roi, lim1 = roi * roi;
 
   for (;;) {
-    // ---- refresh dirty groups and publish this CTA's maximum --------------
+    const int par = rounds & 1;
+    // ---- A. refresh dirty groups; publish this CTA's top-K keys -------------
     for (int g = warp; g < ngroups; g += nwarps) {
       if (!s_dirty[g]) continue;
-      const int s = g * 32 + lane;
-      unsigned long long key = 0;
-      if (s < my_slots && !s_used[s]) key = make_key(s_area[s], s * G + k);
-#pragma unroll
-      for (int o = 16; o > 0; o >>= 1) {
-        const unsigned long long w = __shfl_xor_sync(0xffffffffu, key, o);
-        key = w > key ? w : key;
-      }
+      const unsigned long long key = group_key(s_area, s_flag, g, lane, my_slots, G, k);
       if (lane == 0) {
         s_gmax[g] = key;
         s_dirty[g] = 0;
@@ -217,225 +218,401 @@ __global__ void __launch_bounds__(kSiteThreads, 1) site_kernel(const SiteArgs a)
     }
     __syncthreads();
     if (warp == 0) {
-      unsigned long long key = 0;
-      for (int g = lane; g < ngroups; g += 32) key = s_gmax[g] > key ? s_gmax[g] : key;
+      unsigned long long *out = a.topk + ((size_t)par * G + k) * kTopK * 2;
+      int taken[kTopK];
+      int nt = 0;
+      for (int e = 0; e < kTopK; e++) {
+        unsigned long long key = 0;
+        int gi = -1;
+        for (int g = lane; g < ngroups; g += 32)
+          if (s_gmax[g] > key) {
+            key = s_gmax[g];
+            gi = g;
+          }
 #pragma unroll
-      for (int o = 16; o > 0; o >>= 1) {
-        const unsigned long long w = __shfl_xor_sync(0xffffffffu, key, o);
-        key = w > key ? w : key;
-      }
-      if (lane == 0) {
+        for (int o = 16; o > 0; o >>= 1) {
+          const unsigned long long w = __shfl_xor_sync(0xffffffffu, key, o);
+          const int wg = __shfl_xor_sync(0xffffffffu, gi, o);
+          if (w > key) {
+            key = w;
+            gi = wg;
+          }
+        }
         int pos = 0;
         if (key) {
-          const int c = (int)(0xFFFFFFFFu - (unsigned)(key & 0xFFFFFFFFull));
-          pos = s_pos[c / G];
+          const int s = key_index(key) / G;
+          pos = s_pos[s];
+          if (lane == 0) s_flag[s] |= kTaken;
+          taken[nt++] = s;
+          __syncwarp();
+          const unsigned long long ng = group_key(s_area, s_flag, gi, lane, my_slots, G, k);
+          if (lane == 0) s_gmax[gi] = ng;
+          __syncwarp();
         }
-        unsigned long long *slot = a.slots + ((size_t)(npicks & 1) * G + k) * 2;
-        __stcg(slot, key);
-        __stcg(slot + 1, (unsigned long long)pos);
+        if (lane == 0) {
+          __stcg(out + 2 * e, key);
+          __stcg(out + 2 * e + 1, (unsigned long long)pos);
+        }
+      }
+      // restore the extracted slots and their groups
+      for (int e = 0; e < nt; e++) {
+        const int s = taken[e];
+        if (lane == 0) s_flag[s] &= (unsigned char)~kTaken;
+        __syncwarp();
+        const unsigned long long ng = group_key(s_area, s_flag, s >> 5, lane, my_slots, G, k);
+        if (lane == 0) s_gmax[s >> 5] = ng;
+        __syncwarp();
       }
     }
     mark(1);
-    if (!group_sync(gb, a.err, &s_flag)) return;
+    if (!group_sync(gb, a.err, &s_flagv)) return;
     mark(2);
-    if (npicks > 0) {  // the buffer written last round is complete: read it now
+    {  // the buffer written last round is complete: read it now
       uint64_t *tmp = X;
       X = Y;
       Y = tmp;
-      uint64_t *tb = ncur;
-      ncur = nprev;
-      nprev = tb;
-      prev_px = cur_px;
-      prev_fw = cur_fw;
+    }
+    if (k == 0 && tid < nprev) {  // self-check of last round's picks, then reset
+      int *nc = a.ncount + (1 - par) * kMaxPicks;
+      if (__ldcg(nc + tid) != (int)(s_pkey[tid] >> 32)) atomicOr(a.err, kErrSiteMismatch);
+      __stcg(nc + tid, 0);
     }
 
-    // ---- 1. agree on the pick ---------------------------------------------
-    if (warp * 32 < G) {
-      KeyPos v{0ull, 0};
-      if (tid < G) {
-        const unsigned long long *slot = a.slots + ((size_t)(npicks & 1) * G + tid) * 2;
-        v.key = __ldcg(slot);
-        v.pos = (int)__ldcg(slot + 1);
-      }
-      v = warp_argmax(v);
-      if (lane == 0) {
-        s_rkey[warp] = v.key;
-        s_rpos[warp] = v.pos;
-      }
+    // ---- B. merge the published lists; accept the exact prefix --------------
+    for (int i = tid; i < GK; i += blockDim.x) {
+      const unsigned long long *src = a.topk + ((size_t)par * GK + i) * 2;
+      s_mkey[i] = __ldcg(src);
+      s_mpos[i] = (int)__ldcg(src + 1);
     }
-    if (G > 32) __syncthreads();
+    __syncthreads();
     if (warp == 0) {
-      KeyPos w{0ull, 0};
-      if (lane * 32 < G) {
-        w.key = s_rkey[lane];
-        w.pos = s_rpos[lane];
+      // exactness threshold: unpublished keys are below each full list's last key
+      unsigned long long T = 0;
+      for (int g = lane; g < G; g += 32) {
+        const unsigned long long last = s_mkey[g * kTopK + kTopK - 1];
+        T = last > T ? last : T;
       }
-      w = warp_argmax(w);
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) {
+        const unsigned long long w = __shfl_xor_sync(0xffffffffu, T, o);
+        T = w > T ? w : T;
+      }
+      int head[5];  // list heads of lists lane, lane+32, ... (G <= 160)
+#pragma unroll
+      for (int q = 0; q < 5; q++) head[q] = 0;
+      long long cum = s_cum;
+      int m = 0, stop_at = -1;
+      const int max_m = min(kMaxPicks, a.pair_cap / max(a.pick_cap, 1));
+      while (m < max_m) {
+        unsigned long long key = 0;
+        int idx = -1;
+#pragma unroll
+        for (int q = 0; q < 5; q++) {
+          const int g = lane + 32 * q;
+          if (g < G && head[q] < kTopK) {
+            const int e = g * kTopK + head[q];
+            const unsigned long long v = s_mkey[e];
+            if (v > key) {
+              key = v;
+              idx = e;
+            }
+          }
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+          const unsigned long long w = __shfl_xor_sync(0xffffffffu, key, o);
+          const int e2 = __shfl_xor_sync(0xffffffffu, idx, o);
+          if (w > key) {
+            key = w;
+            idx = e2;
+          }
+        }
+        if (key == 0 || (key >> 32) == 0 || key < T) break;
+        const int pos = s_mpos[idx];
+        // distance to every pick accepted this round
+        const int px = pos / n, py = pos - (pos / n) * n;
+        bool near = false;
+        for (int j = lane; j < m; j += 32) {
+          const int q = s_ppos[j];
+          const int dx = q / n - px, dy = q - (q / n) * n - py;
+          near |= dx * dx + dy * dy <= lim2;
+        }
+        if (__any_sync(0xffffffffu, near)) break;
+        if (lane == 0) {
+          s_pk[m] = key_index(key);
+          s_ppos[m] = pos;
+          s_pkey[m] = key;
+        }
+        {
+          const int g = idx / kTopK;
+          if (lane == (g & 31)) {
+#pragma unroll
+            for (int q = 0; q < 5; q++)
+              if (q == (g >> 5)) head[q]++;
+          }
+        }
+        __syncwarp();
+        cum += (long long)(key >> 32);
+        m++;
+        if (cum >= a.stop_area) {
+          stop_at = m;  // the reference stops after this pick
+          break;
+        }
+      }
       if (lane == 0) {
-        s_bestkey = w.key;
-        s_bestpos = w.pos;
-        s_nlist = 0;
-        s_ncount = 0;
+        s_m = m;
+        s_stop_at = stop_at;
+        s_npair = 0;
       }
     }
     __syncthreads();
     mark(3);
-    const unsigned long long bkey = s_bestkey;
-    const int area = (int)(bkey >> 32);
-    if (area <= 0) break;
-    const int pc = (int)(0xFFFFFFFFu - (unsigned)(bkey & 0xFFFFFFFFull));
-    const int bpos = s_bestpos;
-    cumarea += area;
-    if (tid == 0) {
-      if (pc % G == k) {
-        const int s = pc / G;
-        s_used[s] = 1;
-        s_dirty[s >> 5] = 1;
-        a.selected[pc] = 1;
-      }
-      if (k == 0) a.order[npicks] = pc;
-    }
-    npicks++;
-    if (cumarea >= a.stop_area) break;  // 100.0*cumarea/n^2 > 95 (siting.cpp:602-604)
+    const int m = s_m;
+    if (m == 0) break;  // the largest area is 0
 
-    // ---- 2. newly covered bits of the pick --------------------------------
-    const int px = bpos / n, py = bpos - (bpos / n) * n;
-    int fwp, fbp;
-    shed_align(py - roi, fwp, fbp);
-    cur_px = px;
-    cur_fw = fwp;
-    {
-      const uint64_t *shp = a.sheds + (size_t)pc * per;
-      int cnt = 0;
-      for (int i = tid; i < nr * nbw; i += blockDim.x) {
-        const int prow = i / nbw, j = i - prow * nbw;
-        const int gr = px - roi + prow, W = fwp + j;
-        uint64_t v = 0;
-        if (gr >= 0 && gr < n && W >= 0 && W < cw)
-          v = placed_word(shp + (size_t)prow * nwpr, j, nwpr, fbp) & ~__ldcg(X + (size_t)gr * cw + W);
-        ncur[i] = v;
-        cnt += __popcll(v);
-      }
-#pragma unroll
-      for (int o = 16; o > 0; o >>= 1) cnt += __shfl_xor_sync(0xffffffffu, cnt, o);
-      if (lane == 0 && cnt) atomicAdd(&s_ncount, cnt);
-    }
-
-    // ---- 3a. own unused candidates within 2*roi of the pick ---------------
+    // ---- C. (candidate, pick) pairs: own unused candidates within 2*roi ----
     {
       const float r2f = (float)(2 * roi);
-      const int bxl = max(0, (int)floorf(((float)px - r2f) / a.bs) - 2);
-      const int bxh = min(a.nb - 1, (int)floorf(((float)px + r2f) / a.bs) + 2);
-      const int byl = max(0, (int)floorf(((float)py - r2f) / a.bs) - 2);
-      const int byh = min(a.nb - 1, (int)floorf(((float)py + r2f) / a.bs) + 2);
-      const int run = (byh - byl + 1) * a.npb;  // contiguous indices per block row
-      const int per_run = run / G + 2;
-      const int items = (bxh - bxl + 1) * per_run;
-      const int lim = 4 * roi * roi;
-      for (int i = tid; i < items; i += blockDim.x) {
-        const int r = i / per_run, m = i - r * per_run;
+      for (int i = tid; i < m * a.pick_items; i += blockDim.x) {
+        // walk every pick's block rectangle; items beyond it are skipped
+        const int pi = i % m, it = i / m;
+        const int pos = s_ppos[pi];
+        const int px = pos / n, py = pos - (pos / n) * n;
+        const int bxl = max(0, (int)floorf(((float)px - r2f) / a.bs) - 2);
+        const int bxh = min(a.nb - 1, (int)floorf(((float)px + r2f) / a.bs) + 2);
+        const int byl = max(0, (int)floorf(((float)py - r2f) / a.bs) - 2);
+        const int byh = min(a.nb - 1, (int)floorf(((float)py + r2f) / a.bs) + 2);
+        const int run = (byh - byl + 1) * a.npb;
+        const int per_run = run / G + 2;
+        if (it >= (bxh - bxl + 1) * per_run) continue;
+        const int r = it / per_run, mm = it - r * per_run;
         const int start = ((bxl + r) * a.nb + byl) * a.npb;
-        const int c = start + ((k - start % G) + G) % G + m * G;
+        const int c = start + ((k - start % G) + G) % G + mm * G;
         if (c >= start + run || c >= a.nsheds) continue;
         const int s = c / G;
-        if (s_used[s]) continue;
+        if (s_flag[s] & kUsed) continue;
         const int cp = s_pos[s];
         const int dx = cp / n - px, dy = cp - (cp / n) * n - py;
-        if (dx * dx + dy * dy > lim) continue;
-        const int idx = atomicAdd(&s_nlist, 1);
-        if (idx < a.list_cap) {
-          s_list[idx] = s;
-          s_delta[idx] = 0;
-          s_cov[idx] = 0;
+        if (dx * dx + dy * dy > lim2) continue;
+        const int idx = atomicAdd(&s_npair, 1);
+        if (idx < a.pair_cap) {
+          s_pairslot[idx] = s;
+          s_pairpick[idx] = (unsigned char)pi;
+          s_pairdelta[idx] = 0;
+          s_paircov[idx] = 0;
         } else {
           atomicOr(a.err, kErrCapacity);
         }
       }
     }
     __syncthreads();
-    mark(4);
-    if (tid == 0 && s_ncount != area) atomicOr(a.err, kErrSiteMismatch);
-    const int nlist = min(s_nlist, a.list_cap);
+    const int npair = min(s_npair, a.pair_cap);
 
-    // ---- coverage buffer for next round: this CTA's rows of N_t and N_{t-1}
-    for (int i = tid; i < nr * nbw; i += blockDim.x) {
-      const int prow = i / nbw;
-      if (prow % G != k) continue;
-      const int j = i - prow * nbw;
-      uint64_t v = ncur[i];
-      int gr = cur_px - roi + prow, W = cur_fw + j;
-      if (v && gr >= 0 && gr < n && W >= 0 && W < cw)
-        atomicOr(reinterpret_cast<unsigned long long *>(Y + (size_t)gr * cw + W), v);
-      if (npicks > 1) {
-        v = nprev[i];
-        gr = prev_px - roi + prow;
-        W = prev_fw + j;
-        if (v && gr >= 0 && gr < n && W >= 0 && W < cw)
-          atomicOr(reinterpret_cast<unsigned long long *>(Y + (size_t)gr * cw + W), v);
-      }
-    }
-
-    // ---- 3b. subtract the overlap with N; coverage bit of own cell ----------
-    for (int i = tid; i < nlist * nr; i += blockDim.x) {
+    // ---- D. delta of each pair: |V_c n V_p \ cum| row by row ----------------
+    for (int i = tid; i < npair * nr; i += blockDim.x) {
       const int li = i / nr, r = i - li * nr;
-      const int s = s_list[li];
-      const int cp = s_pos[s];
-      const int cx = cp / n, cy = cp - cx * n;
+      const int s = s_pairslot[li], pi = s_pairpick[li];
+      const int cp = s_pos[s], pp = s_ppos[pi];
+      const int cx = cp / n, cy = cp - cx * n, px = pp / n, py = pp - px * n;
       const int gr = cx - roi + r, prow = gr - (px - roi);
-      if (a.intervis && r == roi) {  // the candidate's own cell: covered after p?
-        int cov = (int)((__ldcg(X + (size_t)cx * cw + (cy >> 6)) >> (63 - (cy & 63))) & 1ull);
-        const int j = (cy >> 6) - fwp;
-        if (!cov && prow >= 0 && prow < nr && j >= 0 && j < nbw)
-          cov = (int)((ncur[prow * nbw + j] >> (63 - (cy & 63))) & 1ull);
-        s_cov[li] = (unsigned char)cov;
+      if (r == roi) {  // own cell: covered by this pick?
+        const int ey = cy - py + roi;
+        int cov = 0;
+        if (prow >= 0 && prow < nr && ey >= 0 && ey < nr)
+          cov = (int)((__ldg(a.sheds + (size_t)s_pk[pi] * per + (size_t)prow * nwpr + (ey >> 6)) >>
+                       (63 - (ey & 63))) & 1ull);
+        s_paircov[li] = (unsigned char)cov;
       }
       if (prow < 0 || prow >= nr || gr < 0 || gr >= n) continue;
-      int fwc, fbc;
+      int fwc, fbc, fwp, fbp;
       shed_align(cy - roi, fwc, fbc);
+      shed_align(py - roi, fwp, fbp);
       const int lwc = (cy + roi) >> 6;
       const int lo = max(max(fwc, fwp), 0), hi = min(min(lwc, fwp + nwpr), cw - 1);
       if (lo > hi) continue;
-      const uint64_t *row = a.sheds + (size_t)(s * G + k) * per + (size_t)r * nwpr;
-      const uint64_t *nrow = ncur + prow * nbw;
+      const uint64_t *crow = a.sheds + (size_t)(s * G + k) * per + (size_t)r * nwpr;
+      const uint64_t *prw = a.sheds + (size_t)s_pk[pi] * per + (size_t)prow * nwpr;
+      const uint64_t *xr = X + (size_t)gr * cw;
       int d = 0;
       for (int W = lo; W <= hi; W++)
-        d += __popcll(placed_word(row, W - fwc, nwpr, fbc) & nrow[W - fwp]);
-      if (d) atomicAdd(&s_delta[li], d);
+        d += __popcll(placed_word(crow, W - fwc, nwpr, fbc) & placed_word(prw, W - fwp, nwpr, fbp) &
+                      ~__ldcg(xr + W));
+      if (d) atomicAdd(&s_pairdelta[li], d);
     }
     __syncthreads();
+    mark(4);
+
+    // ---- E. intervis: where would a newly covered candidate overtake? --------
+    int mcut = m;
+    if (a.intervis) {
+      if (tid == 0) s_roundcut = m;
+      __syncthreads();
+      for (int li = tid; li < npair; li += blockDim.x) {
+        const int s = s_pairslot[li];
+        if (!(s_flag[s] & kInel) || !s_paircov[li]) continue;
+        const int j = s_pairpick[li];  // the pick covering s (at most one can)
+        const int c = s * G + k;
+        // this candidate's deltas by pick (picks are > 2roi apart, so only a
+        // few can be within 2roi of it; more than 8 falls back to cutting at
+        // the first position it could matter, which is always safe)
+        int dpick[8], dval[8], nd = 0;
+        bool many = false;
+        for (int l2 = 0; l2 < npair; l2++)
+          if (s_pairslot[l2] == s) {
+            if (nd < 8) {
+              dpick[nd] = s_pairpick[l2];
+              dval[nd] = s_pairdelta[l2];
+              nd++;
+            } else {
+              many = true;
+            }
+          }
+        int cut = m;
+        if (many) {
+          cut = j + 1;
+        } else {
+          for (int q = j + 1; q < m; q++) {  // gain after picks 0..q-1
+            int g = s_gain[s];
+            for (int e = 0; e < nd; e++)
+              if (dpick[e] < q) g -= dval[e];
+            if (make_key(g, c) > s_pkey[q]) {
+              cut = q;
+              break;
+            }
+          }
+        }
+        if (cut < m) atomicMin(&s_roundcut, cut);
+      }
+      __syncthreads();
+      if (tid == 0) __stcg(a.cuts + par * G + k, s_roundcut);
+      if (!group_sync(gb, a.err, &s_flagv)) return;
+      if (warp == 0) {
+        int c = m;
+        for (int g = lane; g < G; g += 32) c = min(c, __ldcg(a.cuts + par * G + g));
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) c = min(c, __shfl_xor_sync(0xffffffffu, c, o));
+        if (lane == 0) s_mcut = c;
+      }
+      __syncthreads();
+      mcut = s_mcut;
+    }
     mark(5);
 
-    // ---- 4. new gains, intervis gate, dirty groups --------------------------
-    for (int li = tid; li < nlist; li += blockDim.x) {
-      const int s = s_list[li];
-      const int g = s_gain[s] - s_delta[li];
-      s_gain[s] = g;
-      s_area[s] = (!a.intervis || s_cov[li]) ? g : 0;
-      s_dirty[s >> 5] = 1;
+    // ---- F. apply picks 0..mcut-1 -------------------------------------------
+    for (int i = tid; i < mcut; i += blockDim.x) {
+      const int c = s_pk[i];
+      if (c % G == k) {
+        const int s = c / G;
+        s_flag[s] |= kUsed;
+        s_dirty[s >> 5] = 1;
+        a.selected[c] = 1;
+      }
+      if (k == 0) a.order[npicks + i] = c;
+    }
+    for (int li = tid; li < npair; li += blockDim.x) {
+      if (s_pairpick[li] >= mcut) continue;
+      const int s = s_pairslot[li];
+      atomicAdd(&s_dacc[s], s_pairdelta[li]);
+      atomicOr(reinterpret_cast<unsigned *>(s_tag + (s & ~3)),
+               (1u | (s_paircov[li] ? 2u : 0u)) << (8 * (s & 3)));
+    }
+    // coverage buffer for next round: placed sheds of last round's and this
+    // round's picks, rows spread over the CTAs
+    {
+      const int nb2 = nwpr + 1;
+      const int tot = (nprev + mcut) * nr * nb2;
+      for (int i = tid; i < tot; i += blockDim.x) {
+        const int pi = i / (nr * nb2), rem = i - pi * nr * nb2;
+        const int prow = rem / nb2, j = rem - prow * nb2;
+        if (prow % G != k) continue;
+        const bool cur = pi >= nprev;
+        const int pos = cur ? s_ppos[pi - nprev] : s_prevpos[pi];
+        const int c = cur ? s_pk[pi - nprev] : s_prevpk[pi];
+        const int px = pos / n, py = pos - px * n;
+        int fwp, fbp;
+        shed_align(py - roi, fwp, fbp);
+        const int gr = px - roi + prow, W = fwp + j;
+        if (gr < 0 || gr >= n || W < 0 || W >= cw) continue;
+        const uint64_t v = placed_word(a.sheds + (size_t)c * per + (size_t)prow * nwpr, j, nwpr, fbp);
+        if (!v) continue;
+        atomicOr(reinterpret_cast<unsigned long long *>(Y + (size_t)gr * cw + W), v);
+        if (cur) {
+          const int cnt = __popcll(v & ~__ldcg(X + (size_t)gr * cw + W));
+          if (cnt) atomicAdd(a.ncount + par * kMaxPicks + (pi - nprev), cnt);
+        }
+      }
+    }
+    __syncthreads();
+    for (int li = tid; li < npair; li += blockDim.x) {
+      if (s_pairpick[li] >= mcut) continue;
+      const int s = s_pairslot[li];
+      const unsigned char tag = s_tag[s];
+      if (!(tag & 1)) continue;  // already applied through another pair
+      if (atomicAnd(reinterpret_cast<unsigned *>(s_tag + (s & ~3)), ~(0xFFu << (8 * (s & 3)))) &
+          (1u << (8 * (s & 3)))) {
+        // first pair of this candidate: apply its summed delta once
+        const int g = s_gain[s] - s_dacc[s];
+        s_gain[s] = g;
+        s_dacc[s] = 0;
+        bool cov = (tag & 2) != 0;
+        if (a.intervis && !cov) {
+          const int cp = s_pos[s];
+          const int cx = cp / n, cy = cp - cx * n;
+          cov = (__ldcg(X + (size_t)cx * cw + (cy >> 6)) >> (63 - (cy & 63))) & 1ull;
+        }
+        const bool inel = a.intervis && !cov;
+        s_area[s] = inel ? 0 : g;
+        s_flag[s] = (unsigned char)((s_flag[s] & ~kInel) | (inel ? kInel : 0));
+        s_dirty[s >> 5] = 1;
+      }
+    }
+    if (tid < mcut) {
+      s_prevpos[tid] = s_ppos[tid];
+      s_prevpk[tid] = s_pk[tid];
+    }
+    if (tid == 0) {
+      long long cadd = 0;
+      for (int i = 0; i < mcut; i++) cadd += (long long)(s_pkey[i] >> 32);
+      s_cum += cadd;
+      s_done = (s_stop_at > 0 && s_stop_at <= mcut) ? 1 : 0;
     }
     __syncthreads();
     mark(6);
+    npicks += mcut;
+    nprev = mcut;
+    rounds++;
+    if (s_done) break;
   }
 
   if (k == 0 && tid == 0) {
     a.out[0] = npicks;
-    a.out[1] = cumarea;
-    a.out[2] = npicks;
+    a.out[1] = s_cum;
+    a.out[2] = rounds;
     for (int i = 0; i < 7; i++) a.out[3 + i] = ph[i];
   }
 }
 
-struct SiteGeomLimits {
-  int list_cap;
+// Bounds of the neighbour search around one pick: the block rectangle
+// spans at most ceil((4roi+1)/bs)+6 block rows and columns (the kernel's +-2
+// margins), and a CTA owns every G-th index of each contiguous block-row run.
+struct PickBounds {
+  int items;  // enumeration items per pick
+  int cap;    // own candidates near one pick
 };
 
-int site_list_cap(int roi, int nsheds, int G, int nb, int npb, float bs) {
-  const int span_blocks = (int)std::ceil((4.0 * roi + 1.0) / bs) + 4;
-  const int nbx = std::min(nb, span_blocks);
-  const int run = std::min(nb, span_blocks) * npb;
-  long long cap = (long long)nbx * (run / G + 2);
-  cap = std::min<long long>(cap, (nsheds + G - 1) / G);
-  return (int)std::max<long long>(cap, 1);
+PickBounds site_pick_bounds(int roi, int nsheds, int G, int nb, int npb, float bs) {
+  const int span = (int)std::ceil((4.0 * roi + 1.0) / bs) + 6;
+  const int nbx = std::min(nb, span);
+  const long long run = (long long)std::min(nb, span) * npb;
+  const long long items = (long long)nbx * (run / G + 2);
+  PickBounds b;
+  b.items = (int)std::min<long long>(items, 1 << 30);
+  b.cap = (int)std::max<long long>(1, std::min<long long>(items, (nsheds + G - 1) / G));
+  return b;
+}
+
+int site_pair_cap(const PickBounds &b) {
+  return (int)std::min<long long>(kMaxPairs, (long long)b.cap * kMaxPicks);
 }
 
 }  // namespace
@@ -458,56 +635,78 @@ long long site_stop_area(int nrows) {
   return lo;
 }
 
-size_t site_scratch_bytes(int nrows, int nsheds, int nctas) {
+namespace {
+
+size_t scratch_layout(int nrows, int nsheds, int nctas, unsigned char *base, SiteScratch *s) {
   const size_t cw = (size_t)(nrows + 63) / 64;
-  size_t b = 2 * (size_t)nrows * cw * 8;
-  b += (size_t)2 * nctas * 2 * 8;
-  b += 256;  // barrier + out
-  b += 2 * (((size_t)nsheds * 4 + 255) & ~(size_t)255);  // order + gains
-  return b + 1024;
+  size_t off = 0;
+  auto take = [&](size_t bytes) {
+    unsigned char *q = base ? base + off : nullptr;
+    off += (bytes + 255) & ~(size_t)255;
+    return q;
+  };
+  unsigned char *c0 = take((size_t)nrows * cw * 8);
+  unsigned char *c1 = take((size_t)nrows * cw * 8);
+  unsigned char *tk = take((size_t)2 * nctas * kTopK * 2 * 8);
+  unsigned char *cu = take((size_t)2 * nctas * 4);
+  unsigned char *nc = take((size_t)2 * kMaxPicks * 4);
+  unsigned char *br = take(64);
+  unsigned char *ou = take(128);
+  unsigned char *od = take((size_t)nsheds * 4);
+  unsigned char *gn = take((size_t)nsheds * 4);
+  if (s) {
+    s->cum[0] = reinterpret_cast<uint64_t *>(c0);
+    s->cum[1] = reinterpret_cast<uint64_t *>(c1);
+    s->topk = reinterpret_cast<unsigned long long *>(tk);
+    s->cuts = reinterpret_cast<int *>(cu);
+    s->ncount = reinterpret_cast<int *>(nc);
+    s->bar = reinterpret_cast<unsigned *>(br);
+    s->out = reinterpret_cast<long long *>(ou);
+    s->order = reinterpret_cast<int32_t *>(od);
+    s->gains = reinterpret_cast<int32_t *>(gn);
+  }
+  return off;
+}
+
+size_t round16(size_t b) { return (b + 15) & ~(size_t)15; }
+
+}  // namespace
+
+size_t site_scratch_bytes(int nrows, int nsheds, int nctas) {
+  return scratch_layout(nrows, nsheds, nctas, nullptr, nullptr);
 }
 
 void site_carve_scratch(void *base, int nrows, int nsheds, int nctas, SiteScratch *s) {
-  const size_t cw = (size_t)(nrows + 63) / 64;
-  unsigned char *p = static_cast<unsigned char *>(base);
-  auto take = [&](size_t bytes) {
-    unsigned char *q = p;
-    p += (bytes + 255) & ~(size_t)255;
-    return q;
-  };
-  s->cum[0] = reinterpret_cast<uint64_t *>(take((size_t)nrows * cw * 8));
-  s->cum[1] = reinterpret_cast<uint64_t *>(take((size_t)nrows * cw * 8));
-  s->slots = reinterpret_cast<uint64_t *>(take((size_t)2 * nctas * 2 * 8));
-  s->bar = reinterpret_cast<unsigned *>(take(64));
-  s->out = reinterpret_cast<long long *>(take(64));
-  s->order = reinterpret_cast<int32_t *>(take((size_t)nsheds * 4));
-  s->gains = reinterpret_cast<int32_t *>(take((size_t)nsheds * 4));
+  scratch_layout(nrows, nsheds, nctas, static_cast<unsigned char *>(base), s);
 }
 
-// Few CTAs keep the per-round barrier and the redundant reads of the pick's
-// shed cheap; enough CTAs keep each one's candidates within kMaxSlots.
+// One CTA per SM: the per-round work is spread as widely as possible, and the
+// merged top-K lists (G * kTopK keys) stay small enough to walk with one warp.
 int site_default_ctas(int nsheds, int sm_count) {
-  int g = std::max(32, (nsheds + kMaxSlots - 1) / kMaxSlots);
-  g = std::min(g, std::max(1, nsheds));
-  return std::min(g, sm_count);
+  int g = std::max(1, std::min(nsheds, sm_count));
+  g = std::max(g, (nsheds + kMaxSlots - 1) / kMaxSlots);
+  return std::min(g, std::min(sm_count, 160));
 }
 
 size_t site_smem_bytes(int roi, int nsheds, int nctas, int nblocks, int npb, float blocksize) {
-  const int nr = 2 * roi + 1, nwpr = (nr + 63) / 64, nbw = nwpr + 1;
+  (void)roi;
   const int nslots = (nsheds + nctas - 1) / nctas;
   const int ngroups = (nslots + 31) / 32;
-  const int cap = site_list_cap(roi, nsheds, nctas, nblocks, npb, blocksize);
-  size_t b = 2 * (size_t)nr * nbw * 8;
-  b += (size_t)ngroups * 8;
-  b += (size_t)nslots * 12;
-  b += (size_t)cap * 9;
-  b += nslots + ngroups;
-  return (b + 15) & ~(size_t)15;
+  const int GK = nctas * kTopK;
+  const PickBounds pb = site_pick_bounds(roi, nsheds, nctas, nblocks, npb, blocksize);
+  const int pair_cap = site_pair_cap(pb);
+  size_t b = 0;
+  b += round16((size_t)ngroups * 8) + round16((size_t)GK * 8) + round16(kMaxPicks * 8);
+  b += 4 * round16((size_t)nslots * 4);
+  b += round16((size_t)GK * 4) + 4 * round16(kMaxPicks * 4);
+  b += 2 * round16((size_t)pair_cap * 4) + 2 * round16((size_t)pair_cap);
+  b += 2 * round16((size_t)nslots) + round16((size_t)ngroups);
+  return b;
 }
 
 bool site_supported(int roi, int nsheds, int nctas) {
   const int nslots = (nsheds + nctas - 1) / nctas;
-  return nslots <= kMaxSlots && roi <= 1000;
+  return nslots <= kMaxSlots && nctas <= 160 && roi <= 2000;
 }
 
 cudaError_t launch_site(int nrows, int roi, int intervis, int nsheds, const int32_t *obs,
@@ -527,7 +726,9 @@ cudaError_t launch_site(int nrows, int roi, int intervis, int nsheds, const int3
   a.npb = npb;
   a.cum0 = s.cum[0];
   a.cum1 = s.cum[1];
-  a.slots = reinterpret_cast<unsigned long long *>(s.slots);
+  a.topk = s.topk;
+  a.cuts = s.cuts;
+  a.ncount = s.ncount;
   a.bar = s.bar;
   a.out = s.out;
   a.order = s.order;
@@ -535,7 +736,10 @@ cudaError_t launch_site(int nrows, int roi, int intervis, int nsheds, const int3
   a.gains = s.gains;
   a.err = d_err;
   a.nslots = (nsheds + nctas - 1) / nctas;
-  a.list_cap = site_list_cap(roi, nsheds, nctas, nblocks, npb, blocksize);
+  const PickBounds pb = site_pick_bounds(roi, nsheds, nctas, nblocks, npb, blocksize);
+  a.pick_items = pb.items;
+  a.pick_cap = pb.cap;
+  a.pair_cap = site_pair_cap(pb);
   a.stop_area = site_stop_area(nrows);
   const size_t shm = site_smem_bytes(roi, nsheds, nctas, nblocks, npb, blocksize);
   const int nr = 2 * roi + 1, per = nr * ((nr + 63) / 64);
