@@ -40,7 +40,7 @@ namespace {
 
 constexpr int kSiteThreads = 1024;
 constexpr int kMaxSlots = 4096;  // candidates owned by one CTA
-constexpr int kTopK = 8;         // keys each CTA publishes per round
+constexpr int kTopK = 4;         // keys each CTA publishes per round
 constexpr int kMaxPicks = 64;    // picks accepted in one round at most
 constexpr int kMaxPairs = 8192;  // (candidate, pick) pairs one CTA updates per round
 
@@ -50,7 +50,7 @@ struct SiteArgs {
   const uint64_t *sheds;
   float bs;
   int nb, npb;
-  uint64_t *cum0, *cum1;
+  uint64_t *cum0;  // coverage bitmap, updated in place
   unsigned long long *topk;  // [2][G][kTopK] x {key, cell}
   int *cuts;                 // [2][G]: per-CTA cut of the round's prefix (intervis)
   int *ncount;               // [2][kMaxPicks]: popcount of each pick's new bits
@@ -130,17 +130,19 @@ __global__ void __launch_bounds__(256) site_score_kernel(const uint64_t *sheds, 
 
 __global__ void __launch_bounds__(kSiteThreads, 1) site_kernel(const SiteArgs a) {
   extern __shared__ __align__(16) unsigned char sm[];
-  __shared__ int s_m, s_mcut, s_stop_at, s_done, s_npair, s_flagv, s_roundcut;
+  __shared__ int s_m, s_mcut, s_stop_at, s_done, s_flagv, s_roundcut, s_mprev;
   __shared__ long long s_cum;
 
   const int G = a.G, k = blockIdx.x;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nwarps = blockDim.x >> 5;
   const int n = a.n, roi = a.roi, nr = 2 * roi + 1, nwpr = (nr + 63) / 64;
+  const int nch = (nwpr + 1 + 3) / 4;  // 4-word chunks of a placed row (nwpr+1 words)
   const int cw = (n + 63) / 64;
   const size_t per = (size_t)nr * nwpr;
   const int my_slots = k < a.nsheds ? (a.nsheds - k + G - 1) / G : 0;
   const int ngroups = (a.nslots + 31) / 32;
   const int GK = G * kTopK;
+  const int pcap = a.pick_cap;
 
   // shared-memory carve-up (sizes mirrored by site_smem_bytes)
   unsigned char *p = sm;
@@ -149,7 +151,7 @@ __global__ void __launch_bounds__(kSiteThreads, 1) site_kernel(const SiteArgs a)
     p += (bytes + 15) & ~(size_t)15;
     return q;
   };
-  unsigned long long *s_gmax = reinterpret_cast<unsigned long long *>(take((size_t)ngroups * 8));
+  unsigned long long *s_gtop = reinterpret_cast<unsigned long long *>(take((size_t)ngroups * kTopK * 8));
   unsigned long long *s_mkey = reinterpret_cast<unsigned long long *>(take((size_t)GK * 8));
   unsigned long long *s_pkey = reinterpret_cast<unsigned long long *>(take(kMaxPicks * 8));
   int *s_gain = reinterpret_cast<int *>(take((size_t)a.nslots * 4));
@@ -159,12 +161,10 @@ __global__ void __launch_bounds__(kSiteThreads, 1) site_kernel(const SiteArgs a)
   int *s_mpos = reinterpret_cast<int *>(take((size_t)GK * 4));
   int *s_pk = reinterpret_cast<int *>(take(kMaxPicks * 4));    // pick: candidate index
   int *s_ppos = reinterpret_cast<int *>(take(kMaxPicks * 4));  // pick: cell
-  int *s_prevpos = reinterpret_cast<int *>(take(kMaxPicks * 4));
-  int *s_prevpk = reinterpret_cast<int *>(take(kMaxPicks * 4));
-  int *s_pairslot = reinterpret_cast<int *>(take((size_t)a.pair_cap * 4));
+  int *s_pcnt = reinterpret_cast<int *>(take(kMaxPicks * 4));  // own candidates near the pick
+  int *s_pairslot = reinterpret_cast<int *>(take((size_t)a.pair_cap * 4));  // [pick][pcap]
   int *s_pairdelta = reinterpret_cast<int *>(take((size_t)a.pair_cap * 4));
-  unsigned char *s_pairpick = take((size_t)a.pair_cap);
-  unsigned char *s_paircov = take((size_t)a.pair_cap);
+  unsigned char *s_paircov = take((size_t)a.pair_cap);  // bit0 pick covers c, bit1 c covered before
   unsigned char *s_flag = take((size_t)a.nslots);
   unsigned char *s_tag = take((size_t)a.nslots);  // bit0 touched, bit1 covered (this round)
   unsigned char *s_dirty = take((size_t)ngroups);
@@ -197,38 +197,54 @@ __global__ void __launch_bounds__(kSiteThreads, 1) site_kernel(const SiteArgs a)
   if (tid == 0) {
     s_cum = 0;
     s_done = 0;
+    s_mprev = 0;
   }
   __syncthreads();
   mark(0);
 
-  uint64_t *X = a.cum0, *Y = a.cum1;
+  uint64_t *cum = a.cum0;
   int npicks = 0, rounds = 0, nprev = 0;
-  const int lim2 = 4 * roi * roi, lim1 = roi * roi;
+  const int lim2 = 4 * roi * roi;
 
   for (;;) {
     const int par = rounds & 1;
-    // ---- A. refresh dirty groups; publish this CTA's top-K keys -------------
+    // ---- A. per-group top-K of dirty groups; this CTA's top-K ----------------
     for (int g = warp; g < ngroups; g += nwarps) {
       if (!s_dirty[g]) continue;
-      const unsigned long long key = group_key(s_area, s_flag, g, lane, my_slots, G, k);
-      if (lane == 0) {
-        s_gmax[g] = key;
-        s_dirty[g] = 0;
+      const int s = g * 32 + lane;
+      unsigned long long key = 0;
+      if (s < my_slots && !(s_flag[s] & kUsed)) key = make_key(s_area[s], s * G + k);
+      for (int e = 0; e < kTopK; e++) {
+        unsigned long long mx = key;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+          const unsigned long long w = __shfl_xor_sync(0xffffffffu, mx, o);
+          mx = w > mx ? w : mx;
+        }
+        if (lane == 0) s_gtop[g * kTopK + e] = mx;
+        if (key == mx) key = 0;  // keys are unique (the index is part of them)
       }
+      if (lane == 0) s_dirty[g] = 0;
     }
     __syncthreads();
     if (warp == 0) {
       unsigned long long *out = a.topk + ((size_t)par * G + k) * kTopK * 2;
-      int taken[kTopK];
-      int nt = 0;
+      int h0 = 0, h1 = 0, h2 = 0, h3 = 0;  // heads of groups lane, lane+32, lane+64, lane+96
       for (int e = 0; e < kTopK; e++) {
         unsigned long long key = 0;
         int gi = -1;
-        for (int g = lane; g < ngroups; g += 32)
-          if (s_gmax[g] > key) {
-            key = s_gmax[g];
-            gi = g;
+#pragma unroll
+        for (int q = 0; q < 4; q++) {
+          const int g = lane + 32 * q;
+          const int h = q == 0 ? h0 : q == 1 ? h1 : q == 2 ? h2 : h3;
+          if (g < ngroups && h < kTopK) {
+            const unsigned long long v = s_gtop[g * kTopK + h];
+            if (v > key) {
+              key = v;
+              gi = g;
+            }
           }
+        }
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) {
           const unsigned long long w = __shfl_xor_sync(0xffffffffu, key, o);
@@ -238,43 +254,27 @@ __global__ void __launch_bounds__(kSiteThreads, 1) site_kernel(const SiteArgs a)
             gi = wg;
           }
         }
-        int pos = 0;
-        if (key) {
-          const int s = key_index(key) / G;
-          pos = s_pos[s];
-          if (lane == 0) s_flag[s] |= kTaken;
-          taken[nt++] = s;
-          __syncwarp();
-          const unsigned long long ng = group_key(s_area, s_flag, gi, lane, my_slots, G, k);
-          if (lane == 0) s_gmax[gi] = ng;
-          __syncwarp();
+        if (key && lane == (gi & 31)) {
+          const int q = gi >> 5;
+          h0 += q == 0;
+          h1 += q == 1;
+          h2 += q == 2;
+          h3 += q == 3;
         }
         if (lane == 0) {
+          const int pos = key ? s_pos[key_index(key) / G] : 0;
           __stcg(out + 2 * e, key);
           __stcg(out + 2 * e + 1, (unsigned long long)pos);
         }
-      }
-      // restore the extracted slots and their groups
-      for (int e = 0; e < nt; e++) {
-        const int s = taken[e];
-        if (lane == 0) s_flag[s] &= (unsigned char)~kTaken;
-        __syncwarp();
-        const unsigned long long ng = group_key(s_area, s_flag, s >> 5, lane, my_slots, G, k);
-        if (lane == 0) s_gmax[s >> 5] = ng;
-        __syncwarp();
       }
     }
     mark(1);
     if (!group_sync(gb, a.err, &s_flagv)) return;
     mark(2);
-    {  // the buffer written last round is complete: read it now
-      uint64_t *tmp = X;
-      X = Y;
-      Y = tmp;
-    }
-    if (k == 0 && tid < nprev) {  // self-check of last round's picks, then reset
+    if (k == 0 && tid < s_mprev) {  // self-check of last round's picks, then reset
       int *nc = a.ncount + (1 - par) * kMaxPicks;
-      if (__ldcg(nc + tid) != (int)(s_pkey[tid] >> 32)) atomicOr(a.err, kErrSiteMismatch);
+      if (tid < nprev && __ldcg(nc + tid) != (int)(s_pkey[tid] >> 32))
+        atomicOr(a.err, kErrSiteMismatch);
       __stcg(nc + tid, 0);
     }
 
@@ -284,6 +284,7 @@ __global__ void __launch_bounds__(kSiteThreads, 1) site_kernel(const SiteArgs a)
       s_mkey[i] = __ldcg(src);
       s_mpos[i] = (int)__ldcg(src + 1);
     }
+    if (tid < kMaxPicks) s_pcnt[tid] = 0;
     __syncthreads();
     if (warp == 0) {
       // exactness threshold: unpublished keys are below each full list's last key
@@ -297,20 +298,19 @@ __global__ void __launch_bounds__(kSiteThreads, 1) site_kernel(const SiteArgs a)
         const unsigned long long w = __shfl_xor_sync(0xffffffffu, T, o);
         T = w > T ? w : T;
       }
-      int head[5];  // list heads of lists lane, lane+32, ... (G <= 160)
-#pragma unroll
-      for (int q = 0; q < 5; q++) head[q] = 0;
-      long long cum = s_cum;
+      int h0 = 0, h1 = 0, h2 = 0, h3 = 0, h4 = 0;  // heads of lists lane+32q
+      long long cumv = s_cum;
       int m = 0, stop_at = -1;
-      const int max_m = min(kMaxPicks, a.pair_cap / max(a.pick_cap, 1));
+      const int max_m = min(kMaxPicks, a.pair_cap / max(pcap, 1));
       while (m < max_m) {
         unsigned long long key = 0;
         int idx = -1;
 #pragma unroll
         for (int q = 0; q < 5; q++) {
           const int g = lane + 32 * q;
-          if (g < G && head[q] < kTopK) {
-            const int e = g * kTopK + head[q];
+          const int h = q == 0 ? h0 : q == 1 ? h1 : q == 2 ? h2 : q == 3 ? h3 : h4;
+          if (g < G && h < kTopK) {
+            const int e = g * kTopK + h;
             const unsigned long long v = s_mkey[e];
             if (v > key) {
               key = v;
@@ -329,7 +329,6 @@ __global__ void __launch_bounds__(kSiteThreads, 1) site_kernel(const SiteArgs a)
         }
         if (key == 0 || (key >> 32) == 0 || key < T) break;
         const int pos = s_mpos[idx];
-        // distance to every pick accepted this round
         const int px = pos / n, py = pos - (pos / n) * n;
         bool near = false;
         for (int j = lane; j < m; j += 32) {
@@ -346,15 +345,18 @@ __global__ void __launch_bounds__(kSiteThreads, 1) site_kernel(const SiteArgs a)
         {
           const int g = idx / kTopK;
           if (lane == (g & 31)) {
-#pragma unroll
-            for (int q = 0; q < 5; q++)
-              if (q == (g >> 5)) head[q]++;
+            const int q = g >> 5;
+            h0 += q == 0;
+            h1 += q == 1;
+            h2 += q == 2;
+            h3 += q == 3;
+            h4 += q == 4;
           }
         }
         __syncwarp();
-        cum += (long long)(key >> 32);
+        cumv += (long long)(key >> 32);
         m++;
-        if (cum >= a.stop_area) {
+        if (cumv >= a.stop_area) {
           stop_at = m;  // the reference stops after this pick
           break;
         }
@@ -362,7 +364,6 @@ __global__ void __launch_bounds__(kSiteThreads, 1) site_kernel(const SiteArgs a)
       if (lane == 0) {
         s_m = m;
         s_stop_at = stop_at;
-        s_npair = 0;
       }
     }
     __syncthreads();
@@ -370,11 +371,10 @@ __global__ void __launch_bounds__(kSiteThreads, 1) site_kernel(const SiteArgs a)
     const int m = s_m;
     if (m == 0) break;  // the largest area is 0
 
-    // ---- C. (candidate, pick) pairs: own unused candidates within 2*roi ----
+    // ---- C. own unused candidates within 2*roi of each pick ------------------
     {
       const float r2f = (float)(2 * roi);
       for (int i = tid; i < m * a.pick_items; i += blockDim.x) {
-        // walk every pick's block rectangle; items beyond it are skipped
         const int pi = i % m, it = i / m;
         const int pos = s_ppos[pi];
         const int px = pos / n, py = pos - (pos / n) * n;
@@ -388,95 +388,150 @@ __global__ void __launch_bounds__(kSiteThreads, 1) site_kernel(const SiteArgs a)
         const int r = it / per_run, mm = it - r * per_run;
         const int start = ((bxl + r) * a.nb + byl) * a.npb;
         const int c = start + ((k - start % G) + G) % G + mm * G;
-        if (c >= start + run || c >= a.nsheds) continue;
+        if (c >= start + run || c >= a.nsheds || c == s_pk[pi]) continue;
         const int s = c / G;
         if (s_flag[s] & kUsed) continue;
         const int cp = s_pos[s];
-        const int dx = cp / n - px, dy = cp - (cp / n) * n - py;
+        const int cx = cp / n, cy = cp - (cp / n) * n;
+        const int dx = cx - px, dy = cy - py;
         if (dx * dx + dy * dy > lim2) continue;
-        const int idx = atomicAdd(&s_npair, 1);
-        if (idx < a.pair_cap) {
-          s_pairslot[idx] = s;
-          s_pairpick[idx] = (unsigned char)pi;
-          s_pairdelta[idx] = 0;
-          s_paircov[idx] = 0;
+        const int idx = atomicAdd(&s_pcnt[pi], 1);
+        if (idx < pcap) {
+          const int pr = pi * pcap + idx;
+          s_pairslot[pr] = s;
+          s_pairdelta[pr] = 0;
+          unsigned char cv = 0;
+          if (a.intervis)  // own cell already covered?
+            cv = (unsigned char)(((__ldcg(cum + (size_t)cx * cw + (cy >> 6)) >> (63 - (cy & 63))) & 1ull)
+                                 << 1);
+          s_paircov[pr] = cv;
         } else {
           atomicOr(a.err, kErrCapacity);
         }
       }
     }
     __syncthreads();
-    const int npair = min(s_npair, a.pair_cap);
 
-    // ---- D. delta of each pair: |V_c n V_p \ cum| row by row ----------------
-    for (int i = tid; i < npair * nr; i += blockDim.x) {
-      const int li = i / nr, r = i - li * nr;
-      const int s = s_pairslot[li], pi = s_pairpick[li];
-      const int cp = s_pos[s], pp = s_ppos[pi];
-      const int cx = cp / n, cy = cp - cx * n, px = pp / n, py = pp - px * n;
-      const int gr = cx - roi + r, prow = gr - (px - roi);
-      if (r == roi) {  // own cell: covered by this pick?
-        const int ey = cy - py + roi;
-        int cov = 0;
-        if (prow >= 0 && prow < nr && ey >= 0 && ey < nr)
-          cov = (int)((__ldg(a.sheds + (size_t)s_pk[pi] * per + (size_t)prow * nwpr + (ey >> 6)) >>
-                       (63 - (ey & 63))) & 1ull);
-        s_paircov[li] = (unsigned char)cov;
-      }
-      if (prow < 0 || prow >= nr || gr < 0 || gr >= n) continue;
-      int fwc, fbc, fwp, fbp;
-      shed_align(cy - roi, fwc, fbc);
+    // ---- D. per (pick, row, 4-word chunk): new bits N, pair deltas ----------
+    for (int i = tid; i < m * nr * nch; i += blockDim.x) {
+      const int pi = i / (nr * nch), rem = i - pi * nr * nch;
+      const int prow = rem / nch, ch = rem - prow * nch;
+      const int np = min(s_pcnt[pi], pcap);
+      const bool own_row = (prow % G) == k;
+      if (np == 0 && !own_row) continue;
+      const int pos = s_ppos[pi];
+      const int px = pos / n, py = pos - (pos / n) * n;
+      const int gr = px - roi + prow;
+      if (gr < 0 || gr >= n) continue;
+      int fwp, fbp;
       shed_align(py - roi, fwp, fbp);
-      const int lwc = (cy + roi) >> 6;
-      const int lo = max(max(fwc, fwp), 0), hi = min(min(lwc, fwp + nwpr), cw - 1);
-      if (lo > hi) continue;
-      const uint64_t *crow = a.sheds + (size_t)(s * G + k) * per + (size_t)r * nwpr;
+      const int W0 = fwp + 4 * ch;
       const uint64_t *prw = a.sheds + (size_t)s_pk[pi] * per + (size_t)prow * nwpr;
-      const uint64_t *xr = X + (size_t)gr * cw;
-      int d = 0;
-      for (int W = lo; W <= hi; W++)
-        d += __popcll(placed_word(crow, W - fwc, nwpr, fbc) & placed_word(prw, W - fwp, nwpr, fbp) &
-                      ~__ldcg(xr + W));
-      if (d) atomicAdd(&s_pairdelta[li], d);
+      const uint64_t *xr = cum + (size_t)gr * cw;
+      uint64_t pw[5], N[4];
+#pragma unroll
+      for (int u = 0; u < 5; u++) {
+        const int j = 4 * ch - 1 + u;
+        pw[u] = (j >= 0 && j < nwpr) ? __ldg(prw + j) : 0ull;
+      }
+      int cnt = 0;
+#pragma unroll
+      for (int u = 0; u < 4; u++) {
+        const int W = W0 + u;
+        uint64_t v = (pw[u + 1] >> fbp) | (fbp ? pw[u] << (64 - fbp) : 0ull);
+        const bool ok = (4 * ch + u <= nwpr) && W >= 0 && W < cw;
+        N[u] = ok ? v & ~__ldcg(xr + W) : 0ull;
+        cnt += __popcll(N[u]);
+      }
+      if (own_row && cnt) atomicAdd(a.ncount + par * kMaxPicks + pi, cnt);
+      for (int q = 0; q < np; q++) {
+        const int pr = pi * pcap + q;
+        const int s = s_pairslot[pr];
+        const int cp = s_pos[s];
+        const int cx = cp / n, cy = cp - cx * n;
+        const int r = gr - (cx - roi);
+        if (r < 0 || r >= nr) continue;
+        int fwc, fbc;
+        shed_align(cy - roi, fwc, fbc);
+        const int lwc = (cy + roi) >> 6;
+        if (W0 + 3 < fwc || W0 > lwc) continue;
+        const uint64_t *crow = a.sheds + (size_t)(s * G + k) * per + (size_t)r * nwpr;
+        const int j0 = W0 - fwc - 1;
+        uint64_t cwd[5];
+#pragma unroll
+        for (int u = 0; u < 5; u++) {
+          const int j = j0 + u;
+          cwd[u] = (j >= 0 && j < nwpr) ? __ldg(crow + j) : 0ull;
+        }
+        int d = 0;
+#pragma unroll
+        for (int u = 0; u < 4; u++) {
+          const int W = W0 + u;
+          if (W < fwc || W > lwc) continue;
+          const uint64_t v = (cwd[u + 1] >> fbc) | (fbc ? cwd[u] << (64 - fbc) : 0ull);
+          d += __popcll(v & N[u]);
+        }
+        if (d) atomicAdd(&s_pairdelta[pr], d);
+        if (a.intervis && r == roi) {  // own cell in this chunk: covered by the pick?
+          const int u = (cy >> 6) - W0;
+          if (u >= 0 && u < 4) {
+            const uint64_t v = (pw[u + 1] >> fbp) | (fbp ? pw[u] << (64 - fbp) : 0ull);
+            if ((v >> (63 - (cy & 63))) & 1ull) atomicOr(reinterpret_cast<unsigned *>(s_paircov + (pr & ~3)),
+                                                        1u << (8 * (pr & 3)));
+          }
+        }
+      }
     }
     __syncthreads();
     mark(4);
 
     // ---- E. intervis: where would a newly covered candidate overtake? --------
-    int mcut = m;
+    if (tid == 0) s_roundcut = m;
+    __syncthreads();
     if (a.intervis) {
-      if (tid == 0) s_roundcut = m;
-      __syncthreads();
-      for (int li = tid; li < npair; li += blockDim.x) {
-        const int s = s_pairslot[li];
-        if (!(s_flag[s] & kInel) || !s_paircov[li]) continue;
-        const int j = s_pairpick[li];  // the pick covering s (at most one can)
+      for (int i = tid; i < m * pcap; i += blockDim.x) {
+        const int j = i / pcap, q = i - j * pcap;
+        if (q >= min(s_pcnt[j], pcap)) continue;
+        const int s = s_pairslot[i];
+        if (!(s_flag[s] & kInel) || !(s_paircov[i] & 1)) continue;
         const int c = s * G + k;
-        // this candidate's deltas by pick (picks are > 2roi apart, so only a
-        // few can be within 2roi of it; more than 8 falls back to cutting at
-        // the first position it could matter, which is always safe)
-        int dpick[8], dval[8], nd = 0;
+        // this candidate's deltas by pick: it is within 2roi of few picks, which
+        // are > 2roi apart; more than 8 falls back to cutting at the first
+        // position it could matter, which is always safe
+        int dpick0 = -1, dpick1 = -1, dpick2 = -1, dpick3 = -1, dpick4 = -1, dpick5 = -1;
+        int dval0 = 0, dval1 = 0, dval2 = 0, dval3 = 0, dval4 = 0, dval5 = 0, nd = 0;
         bool many = false;
-        for (int l2 = 0; l2 < npair; l2++)
-          if (s_pairslot[l2] == s) {
-            if (nd < 8) {
-              dpick[nd] = s_pairpick[l2];
-              dval[nd] = s_pairdelta[l2];
+        for (int j2 = 0; j2 < m; j2++) {
+          const int cnt2 = min(s_pcnt[j2], pcap);
+          for (int q2 = 0; q2 < cnt2; q2++)
+            if (s_pairslot[j2 * pcap + q2] == s) {
+              const int dv = s_pairdelta[j2 * pcap + q2];
+              switch (nd) {
+                case 0: dpick0 = j2; dval0 = dv; break;
+                case 1: dpick1 = j2; dval1 = dv; break;
+                case 2: dpick2 = j2; dval2 = dv; break;
+                case 3: dpick3 = j2; dval3 = dv; break;
+                case 4: dpick4 = j2; dval4 = dv; break;
+                case 5: dpick5 = j2; dval5 = dv; break;
+                default: many = true;
+              }
               nd++;
-            } else {
-              many = true;
             }
-          }
+        }
         int cut = m;
         if (many) {
           cut = j + 1;
         } else {
-          for (int q = j + 1; q < m; q++) {  // gain after picks 0..q-1
+          for (int qq = j + 1; qq < m; qq++) {  // gain after picks 0..qq-1
             int g = s_gain[s];
-            for (int e = 0; e < nd; e++)
-              if (dpick[e] < q) g -= dval[e];
-            if (make_key(g, c) > s_pkey[q]) {
-              cut = q;
+            g -= (dpick0 >= 0 && dpick0 < qq) ? dval0 : 0;
+            g -= (dpick1 >= 0 && dpick1 < qq) ? dval1 : 0;
+            g -= (dpick2 >= 0 && dpick2 < qq) ? dval2 : 0;
+            g -= (dpick3 >= 0 && dpick3 < qq) ? dval3 : 0;
+            g -= (dpick4 >= 0 && dpick4 < qq) ? dval4 : 0;
+            g -= (dpick5 >= 0 && dpick5 < qq) ? dval5 : 0;
+            if (make_key(g, c) > s_pkey[qq]) {
+              cut = qq;
               break;
             }
           }
@@ -485,7 +540,10 @@ __global__ void __launch_bounds__(kSiteThreads, 1) site_kernel(const SiteArgs a)
       }
       __syncthreads();
       if (tid == 0) __stcg(a.cuts + par * G + k, s_roundcut);
-      if (!group_sync(gb, a.err, &s_flagv)) return;
+    }
+    // every read of the coverage this round is done once all CTAs pass here
+    if (!group_sync(gb, a.err, &s_flagv)) return;
+    if (a.intervis) {
       if (warp == 0) {
         int c = m;
         for (int g = lane; g < G; g += 32) c = min(c, __ldcg(a.cuts + par * G + g));
@@ -493,9 +551,11 @@ __global__ void __launch_bounds__(kSiteThreads, 1) site_kernel(const SiteArgs a)
         for (int o = 16; o > 0; o >>= 1) c = min(c, __shfl_xor_sync(0xffffffffu, c, o));
         if (lane == 0) s_mcut = c;
       }
-      __syncthreads();
-      mcut = s_mcut;
+    } else if (tid == 0) {
+      s_mcut = m;
     }
+    __syncthreads();
+    const int mcut = s_mcut;
     mark(5);
 
     // ---- F. apply picks 0..mcut-1 -------------------------------------------
@@ -509,43 +569,38 @@ __global__ void __launch_bounds__(kSiteThreads, 1) site_kernel(const SiteArgs a)
       }
       if (k == 0) a.order[npicks + i] = c;
     }
-    for (int li = tid; li < npair; li += blockDim.x) {
-      if (s_pairpick[li] >= mcut) continue;
-      const int s = s_pairslot[li];
-      atomicAdd(&s_dacc[s], s_pairdelta[li]);
+    for (int i = tid; i < mcut * pcap; i += blockDim.x) {
+      const int j = i / pcap, q = i - j * pcap;
+      if (q >= min(s_pcnt[j], pcap)) continue;
+      const int s = s_pairslot[i];
+      atomicAdd(&s_dacc[s], s_pairdelta[i]);
+      const unsigned char cv = s_paircov[i];
       atomicOr(reinterpret_cast<unsigned *>(s_tag + (s & ~3)),
-               (1u | (s_paircov[li] ? 2u : 0u)) << (8 * (s & 3)));
+               (1u | ((cv & 1) ? 2u : 0u) | ((cv & 2) ? 4u : 0u)) << (8 * (s & 3)));
     }
-    // coverage buffer for next round: placed sheds of last round's and this
-    // round's picks, rows spread over the CTAs
+    // coverage: OR this CTA's rows of the accepted picks' placed sheds
     {
       const int nb2 = nwpr + 1;
-      const int tot = (nprev + mcut) * nr * nb2;
-      for (int i = tid; i < tot; i += blockDim.x) {
-        const int pi = i / (nr * nb2), rem = i - pi * nr * nb2;
-        const int prow = rem / nb2, j = rem - prow * nb2;
-        if (prow % G != k) continue;
-        const bool cur = pi >= nprev;
-        const int pos = cur ? s_ppos[pi - nprev] : s_prevpos[pi];
-        const int c = cur ? s_pk[pi - nprev] : s_prevpk[pi];
-        const int px = pos / n, py = pos - px * n;
+      const int rows_mine = k < nr ? (nr - k + G - 1) / G : 0;
+      for (int i = tid; i < mcut * rows_mine * nb2; i += blockDim.x) {
+        const int pi = i / (rows_mine * nb2), rem = i - pi * rows_mine * nb2;
+        const int prow = k + G * (rem / nb2), j = rem % nb2;
+        const int pos = s_ppos[pi];
+        const int px = pos / n, py = pos - (pos / n) * n;
         int fwp, fbp;
         shed_align(py - roi, fwp, fbp);
         const int gr = px - roi + prow, W = fwp + j;
         if (gr < 0 || gr >= n || W < 0 || W >= cw) continue;
-        const uint64_t v = placed_word(a.sheds + (size_t)c * per + (size_t)prow * nwpr, j, nwpr, fbp);
-        if (!v) continue;
-        atomicOr(reinterpret_cast<unsigned long long *>(Y + (size_t)gr * cw + W), v);
-        if (cur) {
-          const int cnt = __popcll(v & ~__ldcg(X + (size_t)gr * cw + W));
-          if (cnt) atomicAdd(a.ncount + par * kMaxPicks + (pi - nprev), cnt);
-        }
+        const uint64_t v =
+            placed_word(a.sheds + (size_t)s_pk[pi] * per + (size_t)prow * nwpr, j, nwpr, fbp);
+        if (v) atomicOr(reinterpret_cast<unsigned long long *>(cum + (size_t)gr * cw + W), v);
       }
     }
     __syncthreads();
-    for (int li = tid; li < npair; li += blockDim.x) {
-      if (s_pairpick[li] >= mcut) continue;
-      const int s = s_pairslot[li];
+    for (int i = tid; i < mcut * pcap; i += blockDim.x) {
+      const int j = i / pcap, q = i - j * pcap;
+      if (q >= min(s_pcnt[j], pcap)) continue;
+      const int s = s_pairslot[i];
       const unsigned char tag = s_tag[s];
       if (!(tag & 1)) continue;  // already applied through another pair
       if (atomicAnd(reinterpret_cast<unsigned *>(s_tag + (s & ~3)), ~(0xFFu << (8 * (s & 3)))) &
@@ -554,27 +609,18 @@ __global__ void __launch_bounds__(kSiteThreads, 1) site_kernel(const SiteArgs a)
         const int g = s_gain[s] - s_dacc[s];
         s_gain[s] = g;
         s_dacc[s] = 0;
-        bool cov = (tag & 2) != 0;
-        if (a.intervis && !cov) {
-          const int cp = s_pos[s];
-          const int cx = cp / n, cy = cp - cx * n;
-          cov = (__ldcg(X + (size_t)cx * cw + (cy >> 6)) >> (63 - (cy & 63))) & 1ull;
-        }
-        const bool inel = a.intervis && !cov;
+        const bool inel = a.intervis && !(tag & 6);
         s_area[s] = inel ? 0 : g;
         s_flag[s] = (unsigned char)((s_flag[s] & ~kInel) | (inel ? kInel : 0));
         s_dirty[s >> 5] = 1;
       }
-    }
-    if (tid < mcut) {
-      s_prevpos[tid] = s_ppos[tid];
-      s_prevpk[tid] = s_pk[tid];
     }
     if (tid == 0) {
       long long cadd = 0;
       for (int i = 0; i < mcut; i++) cadd += (long long)(s_pkey[i] >> 32);
       s_cum += cadd;
       s_done = (s_stop_at > 0 && s_stop_at <= mcut) ? 1 : 0;
+      s_mprev = m;
     }
     __syncthreads();
     mark(6);
@@ -689,17 +735,16 @@ int site_default_ctas(int nsheds, int sm_count) {
 }
 
 size_t site_smem_bytes(int roi, int nsheds, int nctas, int nblocks, int npb, float blocksize) {
-  (void)roi;
   const int nslots = (nsheds + nctas - 1) / nctas;
   const int ngroups = (nslots + 31) / 32;
   const int GK = nctas * kTopK;
   const PickBounds pb = site_pick_bounds(roi, nsheds, nctas, nblocks, npb, blocksize);
   const int pair_cap = site_pair_cap(pb);
   size_t b = 0;
-  b += round16((size_t)ngroups * 8) + round16((size_t)GK * 8) + round16(kMaxPicks * 8);
+  b += round16((size_t)ngroups * kTopK * 8) + round16((size_t)GK * 8) + round16(kMaxPicks * 8);
   b += 4 * round16((size_t)nslots * 4);
-  b += round16((size_t)GK * 4) + 4 * round16(kMaxPicks * 4);
-  b += 2 * round16((size_t)pair_cap * 4) + 2 * round16((size_t)pair_cap);
+  b += round16((size_t)GK * 4) + 3 * round16(kMaxPicks * 4);
+  b += 2 * round16((size_t)pair_cap * 4) + round16((size_t)pair_cap);
   b += 2 * round16((size_t)nslots) + round16((size_t)ngroups);
   return b;
 }
@@ -725,7 +770,6 @@ cudaError_t launch_site(int nrows, int roi, int intervis, int nsheds, const int3
   a.nb = nblocks;
   a.npb = npb;
   a.cum0 = s.cum[0];
-  a.cum1 = s.cum[1];
   a.topk = s.topk;
   a.cuts = s.cuts;
   a.ncount = s.ncount;
