@@ -130,8 +130,11 @@ __global__ void __launch_bounds__(256) site_score_kernel(const uint64_t *sheds, 
 
 __global__ void __launch_bounds__(kSiteThreads, 1) site_kernel(const SiteArgs a) {
   extern __shared__ __align__(16) unsigned char sm[];
-  __shared__ int s_m, s_mcut, s_stop_at, s_done, s_flagv, s_roundcut, s_mprev;
+  __shared__ int s_m, s_mcut, s_stop_at, s_done, s_flagv, s_roundcut, s_mprev, s_nrank;
   __shared__ long long s_cum;
+  __shared__ unsigned long long s_red[32];
+  __shared__ int s_rank[kMaxPicks];
+  __shared__ unsigned char s_near[kMaxPicks];
 
   const int G = a.G, k = blockIdx.x;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nwarps = blockDim.x >> 5;
@@ -271,13 +274,6 @@ __global__ void __launch_bounds__(kSiteThreads, 1) site_kernel(const SiteArgs a)
     mark(1);
     if (!group_sync(gb, a.err, &s_flagv)) return;
     mark(2);
-    if (k == 0 && tid < s_mprev) {  // self-check of last round's picks, then reset
-      int *nc = a.ncount + (1 - par) * kMaxPicks;
-      if (tid < nprev && __ldcg(nc + tid) != (int)(s_pkey[tid] >> 32))
-        atomicOr(a.err, kErrSiteMismatch);
-      __stcg(nc + tid, 0);
-    }
-
     // ---- B. merge the published lists; accept the exact prefix --------------
     for (int i = tid; i < GK; i += blockDim.x) {
       const unsigned long long *src = a.topk + ((size_t)par * GK + i) * 2;
@@ -285,81 +281,77 @@ __global__ void __launch_bounds__(kSiteThreads, 1) site_kernel(const SiteArgs a)
       s_mpos[i] = (int)__ldcg(src + 1);
     }
     if (tid < kMaxPicks) s_pcnt[tid] = 0;
+    if (tid == 0) s_nrank = 0;
     __syncthreads();
-    if (warp == 0) {
-      // exactness threshold: unpublished keys are below each full list's last key
+    {  // exactness threshold: unpublished keys are below each full list's last key
       unsigned long long T = 0;
-      for (int g = lane; g < G; g += 32) {
-        const unsigned long long last = s_mkey[g * kTopK + kTopK - 1];
-        T = last > T ? last : T;
-      }
+      if (tid < G) T = s_mkey[tid * kTopK + kTopK - 1];
 #pragma unroll
       for (int o = 16; o > 0; o >>= 1) {
         const unsigned long long w = __shfl_xor_sync(0xffffffffu, T, o);
         T = w > T ? w : T;
       }
-      int h0 = 0, h1 = 0, h2 = 0, h3 = 0, h4 = 0;  // heads of lists lane+32q
+      if (lane == 0 && warp * 32 < G) s_red[warp] = T;
+    }
+    __syncthreads();
+    unsigned long long T = 0;
+    for (int w = 0; w * 32 < G; w++) T = s_red[w] > T ? s_red[w] : T;
+    // rank of every exactly-ordered entry among the published keys
+    for (int e = tid; e < GK; e += blockDim.x) {
+      const unsigned long long key = s_mkey[e];
+      if (key == 0 || (key >> 32) == 0 || key < T) continue;
+      int rank = 0;
+      for (int f = 0; f < GK; f++) rank += s_mkey[f] > key;
+      if (rank < kMaxPicks) s_rank[rank] = e;
+      atomicAdd(&s_nrank, 1);
+    }
+    __syncthreads();
+    const int nrank = min(s_nrank, kMaxPicks);
+    // a ranked entry is usable if it is > 2roi from every better-ranked one
+    if (tid < nrank) {
+      const int pos = s_mpos[s_rank[tid]];
+      const int px = pos / n, py = pos - (pos / n) * n;
+      bool near = false;
+      for (int j = 0; j < tid; j++) {
+        const int q = s_mpos[s_rank[j]];
+        const int dx = q / n - px, dy = q - (q / n) * n - py;
+        near |= dx * dx + dy * dy <= lim2;
+      }
+      s_near[tid] = near;
+    }
+    __syncthreads();
+    if (warp == 0) {  // prefix length: first near rank, cap, 95% stop
+      const int max_m = min(kMaxPicks, a.pair_cap / max(pcap, 1));
       long long cumv = s_cum;
       int m = 0, stop_at = -1;
-      const int max_m = min(kMaxPicks, a.pair_cap / max(pcap, 1));
-      while (m < max_m) {
-        unsigned long long key = 0;
-        int idx = -1;
+      for (int base = 0; base < nrank && base < max_m; base += 32) {
+        const int r = base + lane;
+        const bool ok = r < nrank && r < max_m && !s_near[r];
+        const unsigned okm = __ballot_sync(0xffffffffu, ok);
+        const int run = okm == 0xffffffffu ? 32 : __ffs(~okm) - 1;  // leading usable ranks
+        // inclusive prefix sums of the areas over this run
+        long long v = (lane < run) ? (long long)(s_mkey[s_rank[r]] >> 32) : 0;
 #pragma unroll
-        for (int q = 0; q < 5; q++) {
-          const int g = lane + 32 * q;
-          const int h = q == 0 ? h0 : q == 1 ? h1 : q == 2 ? h2 : q == 3 ? h3 : h4;
-          if (g < G && h < kTopK) {
-            const int e = g * kTopK + h;
-            const unsigned long long v = s_mkey[e];
-            if (v > key) {
-              key = v;
-              idx = e;
-            }
-          }
+        for (int o = 1; o < 32; o <<= 1) {
+          const long long w = __shfl_up_sync(0xffffffffu, v, o);
+          if (lane >= o) v += w;
         }
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) {
-          const unsigned long long w = __shfl_xor_sync(0xffffffffu, key, o);
-          const int e2 = __shfl_xor_sync(0xffffffffu, idx, o);
-          if (w > key) {
-            key = w;
-            idx = e2;
-          }
-        }
-        if (key == 0 || (key >> 32) == 0 || key < T) break;
-        const int pos = s_mpos[idx];
-        const int px = pos / n, py = pos - (pos / n) * n;
-        bool near = false;
-        for (int j = lane; j < m; j += 32) {
-          const int q = s_ppos[j];
-          const int dx = q / n - px, dy = q - (q / n) * n - py;
-          near |= dx * dx + dy * dy <= lim2;
-        }
-        if (__any_sync(0xffffffffu, near)) break;
-        if (lane == 0) {
-          s_pk[m] = key_index(key);
-          s_ppos[m] = pos;
-          s_pkey[m] = key;
-        }
-        {
-          const int g = idx / kTopK;
-          if (lane == (g & 31)) {
-            const int q = g >> 5;
-            h0 += q == 0;
-            h1 += q == 1;
-            h2 += q == 2;
-            h3 += q == 3;
-            h4 += q == 4;
-          }
-        }
-        __syncwarp();
-        cumv += (long long)(key >> 32);
-        m++;
-        if (cumv >= a.stop_area) {
-          stop_at = m;  // the reference stops after this pick
+        const unsigned hit = __ballot_sync(0xffffffffu, lane < run && cumv + v >= a.stop_area);
+        if (hit) {
+          const int l = __ffs(hit) - 1;
+          m = base + l + 1;
+          stop_at = m;
           break;
         }
+        m = base + run;
+        cumv += __shfl_sync(0xffffffffu, v, 31);
+        if (run < 32) break;
+      }
+      for (int j = lane; j < m; j += 32) {
+        const int e = s_rank[j];
+        s_pk[j] = key_index(s_mkey[e]);
+        s_ppos[j] = s_mpos[e];
+        s_pkey[j] = s_mkey[e];
       }
       if (lane == 0) {
         s_m = m;
@@ -412,74 +404,73 @@ __global__ void __launch_bounds__(kSiteThreads, 1) site_kernel(const SiteArgs a)
     }
     __syncthreads();
 
-    // ---- D. per (pick, row, 4-word chunk): new bits N, pair deltas ----------
-    for (int i = tid; i < m * nr * nch; i += blockDim.x) {
-      const int pi = i / (nr * nch), rem = i - pi * nr * nch;
-      const int prow = rem / nch, ch = rem - prow * nch;
-      const int np = min(s_pcnt[pi], pcap);
-      const bool own_row = (prow % G) == k;
-      if (np == 0 && !own_row) continue;
-      const int pos = s_ppos[pi];
-      const int px = pos / n, py = pos - (pos / n) * n;
-      const int gr = px - roi + prow;
-      if (gr < 0 || gr >= n) continue;
-      int fwp, fbp;
+    // ---- D. per (pair, row, 4-word chunk): |V_c n V_p \ cum| ----------------
+    // Every load of an item is independent (pair cell, pick cell, three rows),
+    // so an item costs one memory latency.  Rows outside the overlap of the
+    // two windows are skipped.
+    for (int i = tid; i < m * pcap * nr * nch; i += blockDim.x) {
+      const int pr = i / (nr * nch), rem = i - pr * nr * nch;
+      const int pi = pr / pcap;
+      if (pr - pi * pcap >= min(s_pcnt[pi], pcap)) continue;
+      const int r = rem / nch, ch = rem - r * nch;
+      const int s = s_pairslot[pr];
+      const int cp = s_pos[s], pp = s_ppos[pi];
+      const int cx = cp / n, cy = cp - cx * n, px = pp / n, py = pp - px * n;
+      const int gr = cx - roi + r, prow = gr - (px - roi);
+      if (prow < 0 || prow >= nr || gr < 0 || gr >= n) continue;
+      int fwc, fbc, fwp, fbp;
+      shed_align(cy - roi, fwc, fbc);
       shed_align(py - roi, fwp, fbp);
-      const int W0 = fwp + 4 * ch;
+      const int lwc = (cy + roi) >> 6;
+      const int lo = max(max(fwc, fwp), 0), hi = min(min(lwc, fwp + nwpr), cw - 1);
+      const int W0 = lo + 4 * ch;
+      const bool own = a.intervis && r == roi;
+      if (W0 > hi && !own) continue;
+      const uint64_t *crow = a.sheds + (size_t)(s * G + k) * per + (size_t)r * nwpr;
       const uint64_t *prw = a.sheds + (size_t)s_pk[pi] * per + (size_t)prow * nwpr;
       const uint64_t *xr = cum + (size_t)gr * cw;
-      uint64_t pw[5], N[4];
+      uint64_t cwd[5], pwd[5], xw[4];
 #pragma unroll
       for (int u = 0; u < 5; u++) {
-        const int j = 4 * ch - 1 + u;
-        pw[u] = (j >= 0 && j < nwpr) ? __ldg(prw + j) : 0ull;
+        const int jc = W0 - fwc - 1 + u, jp = W0 - fwp - 1 + u;
+        cwd[u] = (jc >= 0 && jc < nwpr) ? __ldg(crow + jc) : 0ull;
+        pwd[u] = (jp >= 0 && jp < nwpr) ? __ldg(prw + jp) : 0ull;
       }
-      int cnt = 0;
+#pragma unroll
+      for (int u = 0; u < 4; u++) xw[u] = (W0 + u <= hi) ? __ldcg(xr + W0 + u) : ~0ull;
+      int d = 0;
 #pragma unroll
       for (int u = 0; u < 4; u++) {
-        const int W = W0 + u;
-        uint64_t v = (pw[u + 1] >> fbp) | (fbp ? pw[u] << (64 - fbp) : 0ull);
-        const bool ok = (4 * ch + u <= nwpr) && W >= 0 && W < cw;
-        N[u] = ok ? v & ~__ldcg(xr + W) : 0ull;
-        cnt += __popcll(N[u]);
+        const uint64_t vc = (cwd[u + 1] >> fbc) | (fbc ? cwd[u] << (64 - fbc) : 0ull);
+        const uint64_t vp = (pwd[u + 1] >> fbp) | (fbp ? pwd[u] << (64 - fbp) : 0ull);
+        d += __popcll(vc & vp & ~xw[u]);
       }
-      if (own_row && cnt) atomicAdd(a.ncount + par * kMaxPicks + pi, cnt);
-      for (int q = 0; q < np; q++) {
-        const int pr = pi * pcap + q;
-        const int s = s_pairslot[pr];
-        const int cp = s_pos[s];
-        const int cx = cp / n, cy = cp - cx * n;
-        const int r = gr - (cx - roi);
-        if (r < 0 || r >= nr) continue;
-        int fwc, fbc;
-        shed_align(cy - roi, fwc, fbc);
-        const int lwc = (cy + roi) >> 6;
-        if (W0 + 3 < fwc || W0 > lwc) continue;
-        const uint64_t *crow = a.sheds + (size_t)(s * G + k) * per + (size_t)r * nwpr;
-        const int j0 = W0 - fwc - 1;
-        uint64_t cwd[5];
-#pragma unroll
-        for (int u = 0; u < 5; u++) {
-          const int j = j0 + u;
-          cwd[u] = (j >= 0 && j < nwpr) ? __ldg(crow + j) : 0ull;
-        }
-        int d = 0;
-#pragma unroll
-        for (int u = 0; u < 4; u++) {
-          const int W = W0 + u;
-          if (W < fwc || W > lwc) continue;
-          const uint64_t v = (cwd[u + 1] >> fbc) | (fbc ? cwd[u] << (64 - fbc) : 0ull);
-          d += __popcll(v & N[u]);
-        }
-        if (d) atomicAdd(&s_pairdelta[pr], d);
-        if (a.intervis && r == roi) {  // own cell in this chunk: covered by the pick?
-          const int u = (cy >> 6) - W0;
-          if (u >= 0 && u < 4) {
-            const uint64_t v = (pw[u + 1] >> fbp) | (fbp ? pw[u] << (64 - fbp) : 0ull);
-            if ((v >> (63 - (cy & 63))) & 1ull) atomicOr(reinterpret_cast<unsigned *>(s_paircov + (pr & ~3)),
-                                                        1u << (8 * (pr & 3)));
-          }
-        }
+      if (d) atomicAdd(&s_pairdelta[pr], d);
+      if (own && ch == 0) {  // the candidate's own cell: covered by the pick?
+        const int ey = cy - py + roi;
+        if (ey >= 0 && ey < nr &&
+            ((__ldg(prw + (ey >> 6)) >> (63 - (ey & 63))) & 1ull))
+          atomicOr(reinterpret_cast<unsigned *>(s_paircov + (pr & ~3)), 1u << (8 * (pr & 3)));
+      }
+    }
+    // self-check inputs: new bits of each pick over this CTA's rows, one word
+    // per item
+    {
+      const int nb2 = nwpr + 1;
+      const int rows_mine = k < nr ? (nr - k + G - 1) / G : 0;
+      for (int i = tid; i < m * rows_mine * nb2; i += blockDim.x) {
+        const int pi = i / (rows_mine * nb2), rem = i - pi * rows_mine * nb2;
+        const int prow = k + G * (rem / nb2), j = rem % nb2;
+        const int pp = s_ppos[pi];
+        const int px = pp / n, py = pp - (pp / n) * n;
+        int fwp, fbp;
+        shed_align(py - roi, fwp, fbp);
+        const int gr = px - roi + prow, W = fwp + j;
+        if (gr < 0 || gr >= n || W < 0 || W >= cw) continue;
+        const uint64_t v =
+            placed_word(a.sheds + (size_t)s_pk[pi] * per + (size_t)prow * nwpr, j, nwpr, fbp) &
+            ~__ldcg(cum + (size_t)gr * cw + W);
+        if (v) atomicAdd(a.ncount + par * kMaxPicks + pi, __popcll(v));
       }
     }
     __syncthreads();
@@ -559,6 +550,12 @@ __global__ void __launch_bounds__(kSiteThreads, 1) site_kernel(const SiteArgs a)
     mark(5);
 
     // ---- F. apply picks 0..mcut-1 -------------------------------------------
+    if (k == 0 && tid >= blockDim.x - kMaxPicks) {  // self-check this round, then reset
+      const int i = tid - (blockDim.x - kMaxPicks);
+      int *nc = a.ncount + par * kMaxPicks;
+      if (i < mcut && __ldcg(nc + i) != (int)(s_pkey[i] >> 32)) atomicOr(a.err, kErrSiteMismatch);
+      if (i < m) __stcg(nc + i, 0);
+    }
     for (int i = tid; i < mcut; i += blockDim.x) {
       const int c = s_pk[i];
       if (c % G == k) {
