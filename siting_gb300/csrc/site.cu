@@ -130,11 +130,9 @@ __global__ void __launch_bounds__(256) site_score_kernel(const uint64_t *sheds, 
 
 __global__ void __launch_bounds__(kSiteThreads, 1) site_kernel(const SiteArgs a) {
   extern __shared__ __align__(16) unsigned char sm[];
-  __shared__ int s_m, s_mcut, s_stop_at, s_done, s_flagv, s_roundcut, s_mprev, s_nrank;
+  __shared__ int s_m, s_mcut, s_stop_at, s_done, s_flagv, s_roundcut, s_npair;
   __shared__ long long s_cum;
-  __shared__ unsigned long long s_red[32];
-  __shared__ int s_rank[kMaxPicks];
-  __shared__ unsigned char s_near[kMaxPicks];
+  __shared__ int s_poff[kMaxPicks + 1];
 
   const int G = a.G, k = blockIdx.x;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nwarps = blockDim.x >> 5;
@@ -166,6 +164,7 @@ __global__ void __launch_bounds__(kSiteThreads, 1) site_kernel(const SiteArgs a)
   int *s_ppos = reinterpret_cast<int *>(take(kMaxPicks * 4));  // pick: cell
   int *s_pcnt = reinterpret_cast<int *>(take(kMaxPicks * 4));  // own candidates near the pick
   int *s_pairslot = reinterpret_cast<int *>(take((size_t)a.pair_cap * 4));  // [pick][pcap]
+  int *s_plist = reinterpret_cast<int *>(take((size_t)a.pair_cap * 4));  // dense pair indices
   int *s_pairdelta = reinterpret_cast<int *>(take((size_t)a.pair_cap * 4));
   unsigned char *s_paircov = take((size_t)a.pair_cap);  // bit0 pick covers c, bit1 c covered before
   unsigned char *s_flag = take((size_t)a.nslots);
@@ -200,7 +199,6 @@ __global__ void __launch_bounds__(kSiteThreads, 1) site_kernel(const SiteArgs a)
   if (tid == 0) {
     s_cum = 0;
     s_done = 0;
-    s_mprev = 0;
   }
   __syncthreads();
   mark(0);
@@ -281,77 +279,81 @@ __global__ void __launch_bounds__(kSiteThreads, 1) site_kernel(const SiteArgs a)
       s_mpos[i] = (int)__ldcg(src + 1);
     }
     if (tid < kMaxPicks) s_pcnt[tid] = 0;
-    if (tid == 0) s_nrank = 0;
     __syncthreads();
-    {  // exactness threshold: unpublished keys are below each full list's last key
+    if (warp == 0) {
+      // exactness threshold: unpublished keys are below each full list's last key
       unsigned long long T = 0;
-      if (tid < G) T = s_mkey[tid * kTopK + kTopK - 1];
+      for (int g = lane; g < G; g += 32) {
+        const unsigned long long last = s_mkey[g * kTopK + kTopK - 1];
+        T = last > T ? last : T;
+      }
 #pragma unroll
       for (int o = 16; o > 0; o >>= 1) {
         const unsigned long long w = __shfl_xor_sync(0xffffffffu, T, o);
         T = w > T ? w : T;
       }
-      if (lane == 0 && warp * 32 < G) s_red[warp] = T;
-    }
-    __syncthreads();
-    unsigned long long T = 0;
-    for (int w = 0; w * 32 < G; w++) T = s_red[w] > T ? s_red[w] : T;
-    // rank of every exactly-ordered entry among the published keys
-    for (int e = tid; e < GK; e += blockDim.x) {
-      const unsigned long long key = s_mkey[e];
-      if (key == 0 || (key >> 32) == 0 || key < T) continue;
-      int rank = 0;
-      for (int f = 0; f < GK; f++) rank += s_mkey[f] > key;
-      if (rank < kMaxPicks) s_rank[rank] = e;
-      atomicAdd(&s_nrank, 1);
-    }
-    __syncthreads();
-    const int nrank = min(s_nrank, kMaxPicks);
-    // a ranked entry is usable if it is > 2roi from every better-ranked one
-    if (tid < nrank) {
-      const int pos = s_mpos[s_rank[tid]];
-      const int px = pos / n, py = pos - (pos / n) * n;
-      bool near = false;
-      for (int j = 0; j < tid; j++) {
-        const int q = s_mpos[s_rank[j]];
-        const int dx = q / n - px, dy = q - (q / n) * n - py;
-        near |= dx * dx + dy * dy <= lim2;
-      }
-      s_near[tid] = near;
-    }
-    __syncthreads();
-    if (warp == 0) {  // prefix length: first near rank, cap, 95% stop
-      const int max_m = min(kMaxPicks, a.pair_cap / max(pcap, 1));
+      int h0 = 0, h1 = 0, h2 = 0, h3 = 0, h4 = 0;  // heads of lists lane+32q
       long long cumv = s_cum;
       int m = 0, stop_at = -1;
-      for (int base = 0; base < nrank && base < max_m; base += 32) {
-        const int r = base + lane;
-        const bool ok = r < nrank && r < max_m && !s_near[r];
-        const unsigned okm = __ballot_sync(0xffffffffu, ok);
-        const int run = okm == 0xffffffffu ? 32 : __ffs(~okm) - 1;  // leading usable ranks
-        // inclusive prefix sums of the areas over this run
-        long long v = (lane < run) ? (long long)(s_mkey[s_rank[r]] >> 32) : 0;
+      const int max_m = min(kMaxPicks, a.pair_cap / max(pcap, 1));
+      while (m < max_m) {
+        unsigned long long key = 0;
+        int idx = -1;
 #pragma unroll
-        for (int o = 1; o < 32; o <<= 1) {
-          const long long w = __shfl_up_sync(0xffffffffu, v, o);
-          if (lane >= o) v += w;
+        for (int q = 0; q < 5; q++) {
+          const int g = lane + 32 * q;
+          const int h = q == 0 ? h0 : q == 1 ? h1 : q == 2 ? h2 : q == 3 ? h3 : h4;
+          if (g < G && h < kTopK) {
+            const int e = g * kTopK + h;
+            const unsigned long long v = s_mkey[e];
+            if (v > key) {
+              key = v;
+              idx = e;
+            }
+          }
         }
-        const unsigned hit = __ballot_sync(0xffffffffu, lane < run && cumv + v >= a.stop_area);
-        if (hit) {
-          const int l = __ffs(hit) - 1;
-          m = base + l + 1;
-          stop_at = m;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+          const unsigned long long w = __shfl_xor_sync(0xffffffffu, key, o);
+          const int e2 = __shfl_xor_sync(0xffffffffu, idx, o);
+          if (w > key) {
+            key = w;
+            idx = e2;
+          }
+        }
+        if (key == 0 || (key >> 32) == 0 || key < T) break;
+        const int pos = s_mpos[idx];
+        const int px = pos / n, py = pos - (pos / n) * n;
+        bool near = false;
+        for (int j = lane; j < m; j += 32) {
+          const int q = s_ppos[j];
+          const int dx = q / n - px, dy = q - (q / n) * n - py;
+          near |= dx * dx + dy * dy <= lim2;
+        }
+        if (__any_sync(0xffffffffu, near)) break;
+        if (lane == 0) {
+          s_pk[m] = key_index(key);
+          s_ppos[m] = pos;
+          s_pkey[m] = key;
+        }
+        {
+          const int g = idx / kTopK;
+          if (lane == (g & 31)) {
+            const int q = g >> 5;
+            h0 += q == 0;
+            h1 += q == 1;
+            h2 += q == 2;
+            h3 += q == 3;
+            h4 += q == 4;
+          }
+        }
+        __syncwarp();
+        cumv += (long long)(key >> 32);
+        m++;
+        if (cumv >= a.stop_area) {
+          stop_at = m;  // the reference stops after this pick
           break;
         }
-        m = base + run;
-        cumv += __shfl_sync(0xffffffffu, v, 31);
-        if (run < 32) break;
-      }
-      for (int j = lane; j < m; j += 32) {
-        const int e = s_rank[j];
-        s_pk[j] = key_index(s_mkey[e]);
-        s_ppos[j] = s_mpos[e];
-        s_pkey[j] = s_mkey[e];
       }
       if (lane == 0) {
         s_m = m;
@@ -404,14 +406,41 @@ __global__ void __launch_bounds__(kSiteThreads, 1) site_kernel(const SiteArgs a)
     }
     __syncthreads();
 
+    // compact the pairs: offsets of each pick's pairs, then a dense index list
+    if (warp == 0) {
+      int run = 0;
+      for (int base = 0; base < m; base += 32) {
+        const int j = base + lane;
+        int v = j < m ? min(s_pcnt[j], pcap) : 0;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+          const int w = __shfl_up_sync(0xffffffffu, v, o);
+          if (lane >= o) v += w;
+        }
+        if (j < m) s_poff[j + 1] = run + v;
+        run += __shfl_sync(0xffffffffu, v, 31);
+      }
+      if (lane == 0) {
+        s_poff[0] = 0;
+        s_npair = run;
+      }
+    }
+    __syncthreads();
+    for (int i = tid; i < m * pcap; i += blockDim.x) {
+      const int j = i / pcap, q = i - j * pcap;
+      if (q < min(s_pcnt[j], pcap)) s_plist[s_poff[j] + q] = i;
+    }
+    __syncthreads();
+    const int npair = s_npair;
+
     // ---- D. per (pair, row, 4-word chunk): |V_c n V_p \ cum| ----------------
     // Every load of an item is independent (pair cell, pick cell, three rows),
     // so an item costs one memory latency.  Rows outside the overlap of the
     // two windows are skipped.
-    for (int i = tid; i < m * pcap * nr * nch; i += blockDim.x) {
-      const int pr = i / (nr * nch), rem = i - pr * nr * nch;
+    for (int i = tid; i < npair * nr * nch; i += blockDim.x) {
+      const int u = i / (nr * nch), rem = i - u * nr * nch;
+      const int pr = s_plist[u];
       const int pi = pr / pcap;
-      if (pr - pi * pcap >= min(s_pcnt[pi], pcap)) continue;
       const int r = rem / nch, ch = rem - r * nch;
       const int s = s_pairslot[pr];
       const int cp = s_pos[s], pp = s_ppos[pi];
@@ -480,9 +509,9 @@ __global__ void __launch_bounds__(kSiteThreads, 1) site_kernel(const SiteArgs a)
     if (tid == 0) s_roundcut = m;
     __syncthreads();
     if (a.intervis) {
-      for (int i = tid; i < m * pcap; i += blockDim.x) {
-        const int j = i / pcap, q = i - j * pcap;
-        if (q >= min(s_pcnt[j], pcap)) continue;
+      for (int u = tid; u < npair; u += blockDim.x) {
+        const int i = s_plist[u];
+        const int j = i / pcap;
         const int s = s_pairslot[i];
         if (!(s_flag[s] & kInel) || !(s_paircov[i] & 1)) continue;
         const int c = s * G + k;
@@ -566,9 +595,9 @@ __global__ void __launch_bounds__(kSiteThreads, 1) site_kernel(const SiteArgs a)
       }
       if (k == 0) a.order[npicks + i] = c;
     }
-    for (int i = tid; i < mcut * pcap; i += blockDim.x) {
-      const int j = i / pcap, q = i - j * pcap;
-      if (q >= min(s_pcnt[j], pcap)) continue;
+    for (int u = tid; u < npair; u += blockDim.x) {
+      const int i = s_plist[u];
+      if (i / pcap >= mcut) continue;
       const int s = s_pairslot[i];
       atomicAdd(&s_dacc[s], s_pairdelta[i]);
       const unsigned char cv = s_paircov[i];
@@ -594,9 +623,9 @@ __global__ void __launch_bounds__(kSiteThreads, 1) site_kernel(const SiteArgs a)
       }
     }
     __syncthreads();
-    for (int i = tid; i < mcut * pcap; i += blockDim.x) {
-      const int j = i / pcap, q = i - j * pcap;
-      if (q >= min(s_pcnt[j], pcap)) continue;
+    for (int u = tid; u < npair; u += blockDim.x) {
+      const int i = s_plist[u];
+      if (i / pcap >= mcut) continue;
       const int s = s_pairslot[i];
       const unsigned char tag = s_tag[s];
       if (!(tag & 1)) continue;  // already applied through another pair
@@ -617,7 +646,6 @@ __global__ void __launch_bounds__(kSiteThreads, 1) site_kernel(const SiteArgs a)
       for (int i = 0; i < mcut; i++) cadd += (long long)(s_pkey[i] >> 32);
       s_cum += cadd;
       s_done = (s_stop_at > 0 && s_stop_at <= mcut) ? 1 : 0;
-      s_mprev = m;
     }
     __syncthreads();
     mark(6);
@@ -741,7 +769,7 @@ size_t site_smem_bytes(int roi, int nsheds, int nctas, int nblocks, int npb, flo
   b += round16((size_t)ngroups * kTopK * 8) + round16((size_t)GK * 8) + round16(kMaxPicks * 8);
   b += 4 * round16((size_t)nslots * 4);
   b += round16((size_t)GK * 4) + 3 * round16(kMaxPicks * 4);
-  b += 2 * round16((size_t)pair_cap * 4) + round16((size_t)pair_cap);
+  b += 3 * round16((size_t)pair_cap * 4) + round16((size_t)pair_cap);
   b += 2 * round16((size_t)nslots) + round16((size_t)ngroups);
   return b;
 }
