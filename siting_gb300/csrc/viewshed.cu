@@ -103,9 +103,11 @@ __device__ __forceinline__ void sweep_rays(const Dem &dem, const ShedArgs &a, in
   }
 }
 
-template <bool kSmem>
-__global__ void __launch_bounds__(1024) shed_kernel(const __grid_constant__ CUtensorMap map,
-                                                   const ShedArgs a) {
+// kTwo: CTAs of at most 800 threads, compiled for two resident CTAs per SM
+// (<= 40 registers per thread), so two observers' windows are in flight.
+template <bool kSmem, bool kTwo>
+__global__ void __launch_bounds__(kTwo ? 800 : 1024, kTwo ? 2 : 1)
+    shed_kernel(const __grid_constant__ CUtensorMap map, const ShedArgs a) {
   extern __shared__ __align__(128) unsigned char sm[];
   const int nr = 2 * a.roi + 1, nwpr = (nr + 63) / 64, nwords = nr * nwpr;
   const int ob = a.obs[blockIdx.x];
@@ -211,18 +213,19 @@ cudaError_t launch_sheds(const DemView &dem, int roi, int oht, int tht, int nshe
   ShedPlan eff = plan;
   eff.use_smem = smem;
   const size_t shm = shed_smem_bytes(eff, roi);
+  const bool two = plan.threads <= 800;
+  auto launch = [&](auto kern) -> cudaError_t {
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shm);
+    if (e != cudaSuccess) return e;
+    kern<<<nsheds, plan.threads, shm, st>>>(map, a);
+    return cudaSuccess;
+  };
   cudaError_t e;
-  if (smem) {
-    e = cudaFuncSetAttribute(shed_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             (int)shm);
-    if (e != cudaSuccess) return e;
-    shed_kernel<true><<<nsheds, plan.threads, shm, st>>>(map, a);
-  } else {
-    e = cudaFuncSetAttribute(shed_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             (int)shm);
-    if (e != cudaSuccess) return e;
-    shed_kernel<false><<<nsheds, plan.threads, shm, st>>>(map, a);
-  }
+  if (smem)
+    e = two ? launch(shed_kernel<true, true>) : launch(shed_kernel<true, false>);
+  else
+    e = two ? launch(shed_kernel<false, true>) : launch(shed_kernel<false, false>);
+  if (e != cudaSuccess) return e;
   return cudaGetLastError();
 }
 
