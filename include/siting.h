@@ -156,6 +156,23 @@ int siting_last_pick_order(siting_ctx *ctx, int32_t *order, int cap, int *count)
  * 6 intervis gate and updates).  Writes min(n, 7) values. */
 int siting_last_site_phase_cycles(siting_ctx *ctx, long long *cycles, int n);
 
+/* SITE on device buffers without allocating any memory.  No counterpart in
+ * the reference: it is for callers that cannot allocate device memory on
+ * their call path (a serving loop that reserves its HBM budget at start-up,
+ * or an application whose memory pool already owns the device's memory).
+ * Scratch comes from a 16 MiB array in the library's device image, held by
+ * every GPU that loads the library until the process exits; a job whose
+ * scratch would exceed it returns SITING_ENOMEM, and invalid arguments return
+ * SITING_EINVAL.  Runs on `stream` (a cudaStream_t, NULL = default stream) of
+ * the current device and returns when the results are in `selected` and res.
+ * The first call on a device looks up the array's device address; make that
+ * first call before any stream capture.  All calls share the array: calls
+ * that overlap on the GPU race and must be serialised by the caller. */
+int siting_site_it_noalloc(int nrows, int roi, int intervis, int nsheds,
+                           const int32_t *d_obs, const uint64_t *d_sheds,
+                           uint8_t *d_selected, void *stream,
+                           siting_result *res);
+
 /* ---- whole pipeline (replaces main's stage sequence, siting.cpp:737-759).
  * obs and selected receive nwanted entries (see siting_block_geometry). --- */
 int siting_run(siting_ctx *ctx, const siting_params *p, const uint16_t *elevs,

@@ -138,6 +138,7 @@ def load() -> C.CDLL:
         "siting_calc_sheds_dev": ([_P, i, _P, i, i, i, i, _P, _P], i),
         "siting_site_it": ([_P, i, i, i, i, _P, _P, _P, C.POINTER(_ResultC)], i),
         "siting_site_it_dev": ([_P, i, i, i, i, _P, _P, _P, C.POINTER(_ResultC)], i),
+        "siting_site_it_noalloc": ([i, i, i, i, _P, _P, _P, _P, C.POINTER(_ResultC)], i),
         "siting_run": ([_P, C.POINTER(_ParamsC), _P, _P, _P, C.POINTER(_ResultC)], i),
         "siting_run_dev": ([_P, C.POINTER(_ParamsC), _P, _P, _P, C.POINTER(_ResultC)], i),
         "siting_last_pick_order": ([_P, _P, i, C.POINTER(C.c_int)], i),

@@ -31,9 +31,11 @@
 // shed, 128-bit loads) stream all sheds once at HBM bandwidth.
 #include <algorithm>
 #include <cmath>
+#include <mutex>
 
 #include "common.cuh"
 #include "kernels.h"
+#include "siting.h"
 
 namespace siting {
 namespace {
@@ -827,3 +829,109 @@ cudaError_t launch_site(int nrows, int roi, int intervis, int nsheds, const int3
 }
 
 }  // namespace siting
+
+// ---- allocation-free SITE entry point --------------------------------------
+//
+// Some callers cannot allocate device memory on their call path: a serving
+// loop that reserves its HBM budget at start-up and allows no allocation
+// afterwards, or a host application whose memory pool (for example PyTorch's
+// caching allocator) already owns the device's memory.  For them,
+// siting_site_it_noalloc runs SITE with its scratch (coverage bitmap, CTA key
+// lists, barrier, pick order, round-1 gains, error flag) carved from this
+// file-scope device array instead of cudaMalloc'd workspace.  Every GPU that
+// loads the library holds the array until the process exits.
+//
+// The array is shared by every call on a device and keeps the last call's
+// contents: each call clears what must start at zero.  Calls whose work
+// overlaps on the GPU (different streams, or different host threads) race on
+// it and must be serialised by the caller.
+namespace {
+
+constexpr size_t kNoAllocScratchBytes = size_t(16) << 20;  // 16 MiB per device
+constexpr int kMaxDevices = 64;
+
+}  // namespace
+
+static __device__ __align__(256) unsigned char g_site_noalloc_scratch[kNoAllocScratchBytes];
+
+namespace {
+
+std::mutex g_noalloc_mu;
+void *g_noalloc_base[kMaxDevices] = {};
+
+// Device address of the scratch array on the current device, looked up once
+// per device (host code only sees a host-side stand-in for the symbol).
+int noalloc_scratch(int dev, void **out) {
+  std::lock_guard<std::mutex> lock(g_noalloc_mu);
+  if (!g_noalloc_base[dev]) {
+    void *p = nullptr;
+    if (cudaGetSymbolAddress(&p, g_site_noalloc_scratch) != cudaSuccess || !p) {
+      cudaGetLastError();
+      return SITING_ECUDA;
+    }
+    g_noalloc_base[dev] = p;
+  }
+  *out = g_noalloc_base[dev];
+  return SITING_OK;
+}
+
+}  // namespace
+
+extern "C" int siting_site_it_noalloc(int nrows, int roi, int intervis, int nsheds,
+                                      const int32_t *d_obs, const uint64_t *d_sheds,
+                                      uint8_t *d_selected, void *stream, siting_result *res) {
+  using namespace siting;
+  if (nrows <= 0 || nrows > 20000 || roi < 1 || (intervis != 0 && intervis != 1) || nsheds < 0 ||
+      (nsheds && (!d_obs || !d_sheds || !d_selected)))
+    return SITING_EINVAL;
+  if (res) {
+    res->nusedsheds = 0;
+    res->cumarea = 0;
+    res->coverage = 0.0;
+    res->site_rounds = 0;
+  }
+  if (nsheds == 0) return SITING_OK;
+  int dev = 0, sms = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) return SITING_EDEVICE;
+  if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
+    return SITING_EDEVICE;
+  const int G = site_default_ctas(nsheds, sms);
+  if (!site_supported(roi, nsheds, G)) return SITING_EINVAL;
+  // candidates are taken in any order: one block row holding them all
+  const float bs = (float)nrows;
+  if (site_smem_bytes(roi, nsheds, G, 1, nsheds, bs) > 220 * 1024) return SITING_EINVAL;
+  const size_t need = site_scratch_bytes(nrows, nsheds, G) + 256;  // + error flag
+  if (need > kNoAllocScratchBytes) return SITING_ENOMEM;  // beyond the 16 MiB array
+  void *base = nullptr;
+  int rc = noalloc_scratch(dev, &base);
+  if (rc) return rc;
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  SiteScratch s;
+  site_carve_scratch(base, nrows, nsheds, G, &s);
+  int *d_err = reinterpret_cast<int *>(static_cast<unsigned char *>(base) + need - 256);
+  // zero coverage, key lists, cuts, self-check counters, barrier and outputs
+  if (cudaMemsetAsync(base, 0, (unsigned char *)s.order - (unsigned char *)base, st) != cudaSuccess ||
+      cudaMemsetAsync(d_err, 0, sizeof(int), st) != cudaSuccess ||
+      cudaMemsetAsync(d_selected, 0, nsheds, st) != cudaSuccess)
+    return SITING_ECUDA;
+  if (launch_check_obs(d_obs, nsheds, nrows, d_err, st) != cudaSuccess) return SITING_ECUDA;
+  if (launch_site(nrows, roi, intervis, nsheds, d_obs, d_sheds, bs, 1, nsheds, d_selected, s, G,
+                  d_err, st) != cudaSuccess)
+    return SITING_ECUDA;
+  long long out[3] = {0, 0, 0};
+  int herr = 0;
+  if (cudaMemcpyAsync(out, s.out, sizeof(out), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+      cudaMemcpyAsync(&herr, d_err, sizeof(int), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+      cudaStreamSynchronize(st) != cudaSuccess)
+    return SITING_ECUDA;
+  if (herr & kErrBadInput) return SITING_EINVAL;
+  if (herr & (kErrTmaTimeout | kErrBarrierTimeout)) return SITING_ETIMEOUT;
+  if (herr) return SITING_ECUDA;
+  if (res) {
+    res->nusedsheds = (int)out[0];
+    res->cumarea = out[1];
+    res->coverage = 100.0 * out[1] / ((double)nrows * nrows);
+    res->site_rounds = (int)out[2];
+  }
+  return SITING_OK;
+}
