@@ -221,6 +221,8 @@ def run_gpu(args, w):
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         mean_dev, mean_e2e = t.tolist()
     r = stage[-1]
+    stage_ms = {k: sum(getattr(x, "ms_" + k) for x in stage) / len(stage)
+                for k in ("vix", "findmax", "viewshed", "site")}
     out = {
         "metric": METRIC, "value": world * n * n / (mean_dev / 1e3), "unit": "cells/s",
         "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
@@ -234,33 +236,59 @@ def run_gpu(args, w):
         "e2e": {"value": world * n * n / (mean_e2e / 1e3), "unit": "cells/s",
                 "ms_per_step": mean_e2e, "h2d_bytes_per_step": n * n * 2,
                 "d2h_bytes_per_step": g.nwanted * 5},
-        "gpu_launches": 5 * args.steps,
+        "gpu_launches": 10 * args.steps,  # 5 kernels per job, device and e2e jobs
         "observers_per_s": world * g.nwanted / (mean_dev / 1e3),
-        "stages_ms": {"vix": r.ms_vix, "findmax": r.ms_findmax, "viewshed": r.ms_viewshed,
-                      "site": r.ms_site},
+        "stages_ms": stage_ms,
         "site": {"nusedsheds": r.nusedsheds, "coverage": r.coverage, "rounds": r.site_rounds,
                  "phase_cycles": ctx.last_site_phase_cycles()},
         "clocks": clk,
     }
-    return out, (dem, d_obs, d_sel, r, ctx, g)
+    return out, (dem, d_obs, d_sel, r, ctx, g), stage_ms
 
 
-def roofline(out, w, state, peaks):
-    """Roofline of the dominant stage; also the SITE HBM figure."""
-    dem, d_obs, d_sel, r, ctx, g = state
+# Compulsory HBM bytes per cell / per observer of each stage (DEM read once,
+# outputs written once), the algorithmic traffic the roofline divides by time.
+def stage_bytes(w, nwanted):
     n, roi = w["nrows"], w["roi"]
+    nr = 2 * roi + 1
+    shed = nr * ((nr + 63) // 64) * 8
+    cells = n * n
+    return {
+        "vix": cells * 3,                       # DEM uint16 in, VIX uint8 out
+        "findmax": cells * 1 + nwanted * 4,     # VIX in, observers out
+        "viewshed": cells * 2 + nwanted * (4 + shed),  # DEM + observers in, sheds out
+        "site": nwanted * shed,                 # every shed streamed once (round-1 scores)
+    }
+
+
+def roofline(out, w, state, peaks, stage_ms_mean):
+    """Roofline of the dominant stage (largest mean device time)."""
+    dem, d_obs, d_sel, r, ctx, g = state
     hbm = peaks.get("hbm_gbs", 6800.0)
     src = "measured" if "hbm_gbs" in peaks else "fallback"
+    sb = stage_bytes(w, g.nwanted)
+    stages = {}
+    for k, ms in stage_ms_mean.items():
+        ach = sb[k] / (ms / 1e3) / 1e9
+        stages[k] = {"ms": ms, "alg_bytes": sb[k], "achieved_gbs": ach, "frac": ach / hbm}
+    dom = max(stage_ms_mean, key=stage_ms_mean.get)
+    d = stages[dom]
     obs = d_obs.cpu().numpy()
     order = ctx.last_pick_order(g.nwanted)
-    st = out["stages_ms"]
-    res = {}
-    if order is not None:
-        b = site_algorithmic_bytes(n, roi, obs, order, g.nwanted)
-        ach = b / (st["site"] / 1e3) / 1e9
-        res["site"] = {"bound": "hbm", "achieved": ach, "peak": hbm, "unit": "GB/s",
-                       "frac": ach / hbm, "alg_bytes": b}
-    return res, src
+    site_ref_bytes = site_algorithmic_bytes(w["nrows"], w["roi"], obs, order, g.nwanted)
+    line = {"kernel": dom, "bound": "hbm", "achieved": d["achieved_gbs"], "peak": hbm,
+            "unit": "GB/s", "frac": d["frac"], "traffic": None,
+            "peak_source": f"{src} (MEASURED_PEAKS.json hbm_gbs)" if src == "measured" else
+            "fallback 6800 GB/s"}
+    if dom == "vix":
+        line["note"] = ("VIX is SM-issue bound, not HBM bound: its compulsory traffic is 3 B/cell; "
+                        "see stage_work (line-of-sight samples/s) and profiles/ for issue-slot use")
+    work = {"vix_targets": w["nrows"] ** 2 * w["ntests"],
+            "vix_targets_per_s": w["nrows"] ** 2 * w["ntests"] / (stage_ms_mean["vix"] / 1e3),
+            "site_rounds": r.site_rounds, "site_picks": r.nusedsheds,
+            "site_reference_rescoring_bytes": site_ref_bytes,
+            "site_reference_rescoring_gbs": site_ref_bytes / (stage_ms_mean["site"] / 1e3) / 1e9}
+    return line, stages, work
 
 
 def run_reference(args, w):
@@ -323,7 +351,7 @@ def main():
         print(json.dumps(line))
         return
 
-    out, state = run_gpu(args, w)
+    out, state, stage_ms = run_gpu(args, w)
     if rank != 0:
         return
     peaks = {}
@@ -331,9 +359,10 @@ def main():
     if os.path.exists(pp):
         with open(pp) as f:
             peaks = json.load(f)
-    rl, src = roofline(out, w, state, peaks)
-    out["roofline_stages"] = rl
-    out["peak_source"] = src
+    line, stages, work = roofline(out, w, state, peaks, stage_ms)
+    out["roofline"] = line
+    out["roofline_stages"] = stages
+    out["stage_work"] = work
     if not args.no_cpu_baseline and int(os.environ.get("WORLD_SIZE", "1")) == 1:
         cb = run_reference(argparse.Namespace(warmup=0, steps=1,
                                               cpu_sample_rows=args.cpu_sample_rows), w)

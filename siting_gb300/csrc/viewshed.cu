@@ -36,16 +36,22 @@ struct ShedArgs {
   int *err;
 };
 
+// DEM accessors by linear offset: `base` is the observer cell's offset, a cell
+// (dx, dy) away is at base + dx*stride + dy.
 struct SmemDem {
   const uint16_t *s;
   int w, x0, y0;
-  __device__ __forceinline__ int at(int x, int y) const { return s[(x - x0) * w + (y - y0)]; }
+  __device__ __forceinline__ int base(int x, int y) const { return (x - x0) * w + (y - y0); }
+  __device__ __forceinline__ int stride() const { return w; }
+  __device__ __forceinline__ int at(int o) const { return s[o]; }
 };
 
 struct GlobalDem {
   const uint16_t *g;
   int pitch;
-  __device__ __forceinline__ int at(int x, int y) const { return __ldg(g + x * pitch + y); }
+  __device__ __forceinline__ int base(int x, int y) const { return x * pitch + y; }
+  __device__ __forceinline__ int stride() const { return pitch; }
+  __device__ __forceinline__ int at(int o) const { return __ldg(g + o); }
 };
 
 // Sets bit (row, col) of the shed image held as 32-bit halves of 64-bit words.
@@ -62,7 +68,9 @@ __device__ __forceinline__ void sweep_rays(const Dem &dem, const ShedArgs &a, in
   const int nwpr = (2 * roi + 1 + 63) / 64;
   const int roi2 = roi * roi;
   const int xmin = ox - roi, ymin = oy - roi, xmax = ox + roi, ymax = oy + roi;
-  const int oalt = dem.at(ox, oy) + a.oht;
+  const int W = dem.stride();
+  const int obase = dem.base(ox, oy);
+  const int oalt = dem.at(obase) + a.oht;
   const float foalt = i2f(oalt);
   for (int ip = threadIdx.x; ip < 4 * side; ip += blockDim.x) {
     int tx, ty;
@@ -85,29 +93,46 @@ __device__ __forceinline__ void sweep_rays(const Dem &dem, const ShedArgs &a, in
     const int dmaj = my ? dy : dx, dmin = my ? dx : dy;
     const float slope = fdiv(i2f(dmin), i2f(dmaj));
     const int dir = dmaj > 0 ? 1 : -1;
-    float hs = -99999.f;
-    for (int i = dir; i != dmaj + dir; i += dir) {
-      const int off = round_i(fmul(i2f(i), slope));
-      const int px = my ? ox + off : ox + i;
-      const int py = my ? oy + i : oy + off;
-      if ((unsigned)px >= (unsigned)n || (unsigned)py >= (unsigned)n) break;
-      const int ex = px - ox, ey = py - oy;
-      if (ex * ex + ey * ey > roi2) break;
-      const int pelev = dem.at(px, py);
-      const float fai = i2f(abs(i));
-      const float s = fdiv(i2f(pelev - oalt), fai);
-      if (hs < s) hs = s;
+    // The ray leaves the DEM along the major axis after kedge steps and along
+    // the minor axis when the minor offset leaves [offlo, offhi]; both end it,
+    // as does leaving the roi circle (siting.cpp:333-334).
+    const int omaj = my ? oy : ox, omin = my ? ox : oy;
+    const int kedge = dir > 0 ? n - 1 - omaj : omaj;
+    const int kend = min(dmaj * dir, kedge);
+    const int offlo = -omin, offhi = n - 1 - omin;
+    const int smaj = my ? dir : dir * W, smin = my ? W : 1;
+    const float fdir = dir > 0 ? 1.f : -1.f;
+    float hs = -99999.f, fi = 0.f, fai = 0.f;
+    int moff = 0;
+    for (int k = 1; k <= kend; k++) {
+      fi = fadd(fi, fdir);  // (float)i, i = dir*k: exact
+      fai = fadd(fai, 1.f);  // (float)|i|
+      moff += smaj;
+      const int off = round_i(fmul(fi, slope));
+      if (off < offlo || off > offhi) break;
+      if (k * k + off * off > roi2) break;
+      const int pelev = dem.at(obase + moff + off * smin);
+      const float fa = i2f(pelev - oalt);
+      // s = RN(a/|i|) can exceed hs only if a > hs*|i|; the sign of the fused
+      // hs*|i| - a is exact, so the division runs only when the horizon may rise
+      if (__fmaf_rn(hs, fai, -fa) < 0.f) {
+        const float s = fdiv(fa, fai);
+        if (hs < s) hs = s;
+      }
       const float halt = fadd(foalt, fmul(hs, fai));
-      if (i2f(pelev + a.tht) >= halt) shed_set(bits, nwpr, ex + roi, ey + roi);
+      if (i2f(pelev + a.tht) >= halt) {
+        const int i = dir * k;
+        shed_set(bits, nwpr, (my ? off : i) + roi, (my ? i : off) + roi);
+      }
     }
   }
 }
 
-// kTwo: CTAs of at most 800 threads, compiled for two resident CTAs per SM
-// (<= 40 registers per thread), so two observers' windows are in flight.
-template <bool kSmem, bool kTwo>
-__global__ void __launch_bounds__(kTwo ? 800 : 1024, kTwo ? 2 : 1)
-    shed_kernel(const __grid_constant__ CUtensorMap map, const ShedArgs a) {
+// Two variants: CTAs of at most 800 threads capped at 40 registers per
+// thread, so two CTAs (two observers' windows) are resident per SM; and CTAs
+// of up to 1024 threads for larger roi.
+template <bool kSmem>
+__device__ __forceinline__ void shed_body(const CUtensorMap &map, const ShedArgs &a) {
   extern __shared__ __align__(128) unsigned char sm[];
   const int nr = 2 * a.roi + 1, nwpr = (nr + 63) / 64, nwords = nr * nwpr;
   const int ob = a.obs[blockIdx.x];
@@ -118,7 +143,7 @@ __global__ void __launch_bounds__(kTwo ? 800 : 1024, kTwo ? 2 : 1)
     return;
   }
   const int ox = ob / a.n, oy = ob - (ob / a.n) * a.n;
-  const int hx0 = ox - a.roi, hy0 = (oy - a.roi) & ~7;
+  const int hx0 = ox - a.roi, hy0 = (oy - a.roi) & ~7;  // window origin, 16-byte aligned
   uint16_t *win = reinterpret_cast<uint16_t *>(sm);
   const uint32_t win_bytes = kSmem ? (uint32_t)a.nboxes * a.box_rows * a.win_w * 2u : 0u;
   uint64_t *mbar = reinterpret_cast<uint64_t *>(sm + win_bytes);
@@ -145,6 +170,18 @@ __global__ void __launch_bounds__(kTwo ? 800 : 1024, kTwo ? 2 : 1)
   uint64_t *dst = a.sheds + (size_t)blockIdx.x * nwords;
   const uint64_t *src = reinterpret_cast<const uint64_t *>(bits);
   for (int i = threadIdx.x; i < nwords; i += blockDim.x) dst[i] = src[i];
+}
+
+template <bool kSmem>
+__global__ void __maxnreg__(40)
+    shed_kernel2(const __grid_constant__ CUtensorMap map, const ShedArgs a) {
+  shed_body<kSmem>(map, a);
+}
+
+template <bool kSmem>
+__global__ void __launch_bounds__(1024)
+    shed_kernel1(const __grid_constant__ CUtensorMap map, const ShedArgs a) {
+  shed_body<kSmem>(map, a);
 }
 
 int round8(int v) { return (v + 7) & ~7; }
@@ -222,9 +259,9 @@ cudaError_t launch_sheds(const DemView &dem, int roi, int oht, int tht, int nshe
   };
   cudaError_t e;
   if (smem)
-    e = two ? launch(shed_kernel<true, true>) : launch(shed_kernel<true, false>);
+    e = two ? launch(shed_kernel2<true>) : launch(shed_kernel1<true>);
   else
-    e = two ? launch(shed_kernel<false, true>) : launch(shed_kernel<false, false>);
+    e = two ? launch(shed_kernel2<false>) : launch(shed_kernel1<false>);
   if (e != cudaSuccess) return e;
   return cudaGetLastError();
 }

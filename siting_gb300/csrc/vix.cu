@@ -39,22 +39,28 @@ struct VixArgs {
   int *err;
 };
 
+// DEM accessors by linear offset: `base` is the observer cell's offset, a cell
+// (dx, dy) away is at base + dx*stride + dy.
 struct SmemDem {
   const uint16_t *s;
   int w, x0, y0;
-  __device__ __forceinline__ int at(int x, int y) const { return s[(x - x0) * w + (y - y0)]; }
+  __device__ __forceinline__ int base(int x, int y) const { return (x - x0) * w + (y - y0); }
+  __device__ __forceinline__ int stride() const { return w; }
+  __device__ __forceinline__ int at(int o) const { return s[o]; }
 };
 
 struct GlobalDem {
   const uint16_t *g;
   int pitch;
-  __device__ __forceinline__ int at(int x, int y) const { return __ldg(g + x * pitch + y); }
+  __device__ __forceinline__ int base(int x, int y) const { return x * pitch + y; }
+  __device__ __forceinline__ int stride() const { return pitch; }
+  __device__ __forceinline__ int at(int o) const { return __ldg(g + o); }
 };
 
 // One random target of one cell (siting.cpp:155-175 and 54-135).
 template <class Dem>
-__device__ __forceinline__ int vix_target(const Dem &dem, int n, int roi, int roi2, int tht,
-                                          float span, int ox, int oy, int oz, float foz,
+__device__ __forceinline__ int vix_target(const Dem &dem, int obase, int n, int roi, int roi2,
+                                          int tht, float span, int ox, int oy, int oz, float foz,
                                           uint32_t r1, const float *rtab) {
   const uint32_t r2 = lcg_step(r1);
   // (int)((2*roi+0.99999f)*r/RANDOM_MAX): the divisor is 2^31, so a multiply
@@ -65,30 +71,31 @@ __device__ __forceinline__ int vix_target(const Dem &dem, int n, int roi, int ro
     dx /= 3;
     dy /= 3;
   }
-  const int tx = ox + dx, ty = oy + dy;
-  if ((unsigned)tx >= (unsigned)n || (unsigned)ty >= (unsigned)n) return 0;
+  if ((unsigned)(ox + dx) >= (unsigned)n || (unsigned)(oy + dy) >= (unsigned)n) return 0;
   const int adx = abs(dx), ady = abs(dy);
   if (adx <= 1 && ady <= 1) return 1;
-  const int tz = dem.at(tx, ty) + tht;
+  const int W = dem.stride();
+  const int tz = dem.at(obase + dx * W + dy) + tht;
   const bool mx = adx >= ady;
   const int d = mx ? dx : dy, m = mx ? dy : dx, ad = mx ? adx : ady;
   const float rr = rtab[ad];
   const float drecip = d > 0 ? rr : -rr;
   const float slope = fmul(i2f(m), drecip);
   const float zslope = fmul(i2f(tz - oz), drecip);
-  // Sample offsets are +-1, 2, 4, ...: scaling by a power of two is exact in
-  // FP32, so slope*id and id*zslope are carried by doubling, bit-identical to
-  // the reference's products.
+  // Sample offsets are id = +-1, 2, 4, ... along the major axis: scaling by a
+  // power of two is exact in FP32, so slope*id and id*zslope are carried by
+  // doubling, bit-identical to the reference's products; the sample's offset
+  // from the observer is id*(major stride) + round(slope*id)*(minor stride).
   float sl = d > 0 ? slope : -slope;
   float zs = d > 0 ? zslope : -zslope;
-  const int sx = mx ? (d > 0 ? 1 : -1) : 0, sy = mx ? 0 : (d > 0 ? 1 : -1);
+  int moff = mx ? (d > 0 ? W : -W) : (d > 0 ? 1 : -1);
+  const int smin = mx ? 1 : W;
   for (int step = 1; step < ad; step <<= 1) {
     const int off = round_i(sl);
-    const int x = mx ? ox + sx * step : ox + off;
-    const int y = mx ? oy + off : oy + sy * step;
-    if (i2f(dem.at(x, y)) > fadd(foz, zs)) return 0;
+    if (i2f(dem.at(obase + moff + off * smin)) > fadd(foz, zs)) return 0;
     sl = fadd(sl, sl);
     zs = fadd(zs, zs);
+    moff *= 2;
   }
   return 1;
 }
@@ -102,7 +109,7 @@ __device__ __forceinline__ void vix_tile_work(const Dem &dem, const VixArgs &a, 
   const float span = fadd(i2f(2 * a.roi), 0.99999f);
   const int roi2 = a.roi * a.roi;
   int cell = cb + lane / a.ntests, t = lane % a.ntests;
-  int cur = -1, acc = 0, ox = 0, oy = 0, oz = 0;
+  int cur = -1, acc = 0, ox = 0, oy = 0, oz = 0, obase = 0;
   uint32_t seed = 0;
   float foz = 0.f;
   bool valid = false;
@@ -116,7 +123,8 @@ __device__ __forceinline__ void vix_tile_work(const Dem &dem, const VixArgs &a, 
       oy = ty0 + (cell - lx * T);
       valid = ox < a.n && oy < a.n;
       if (valid) {
-        oz = dem.at(ox, oy) + a.oht;
+        obase = dem.base(ox, oy);
+        oz = dem.at(obase) + a.oht;
         foz = i2f(oz);
         seed = (uint32_t)(ox * a.n + oy);
       }
@@ -124,7 +132,7 @@ __device__ __forceinline__ void vix_tile_work(const Dem &dem, const VixArgs &a, 
     if (valid) {
       const uint2 j = jump[t];
       const uint32_t r1 = (j.x * seed + j.y) & 0x7fffffffu;
-      acc += vix_target(dem, a.n, a.roi, roi2, a.tht, span, ox, oy, oz, foz, r1, rtab);
+      acc += vix_target(dem, obase, a.n, a.roi, roi2, a.tht, span, ox, oy, oz, foz, r1, rtab);
     }
     t += 32;
     while (t >= a.ntests) {
