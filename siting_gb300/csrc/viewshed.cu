@@ -61,6 +61,17 @@ __device__ __forceinline__ void shed_set(unsigned *bits, int nwpr, int row, int 
   atomicOr(&bits[2 * w + (b >> 5)], 1u << (b & 31));
 }
 
+// Same, combining the lanes that hit the same 32-bit word into one atomic: on
+// rays that step along x, a warp's lanes mark neighbouring columns of one row.
+__device__ __forceinline__ void shed_set_warp(unsigned *bits, int nwpr, int row, int col) {
+  const int w = row * nwpr + (col >> 6);
+  const int b = 63 - (col & 63);
+  const int word = 2 * w + (b >> 5);
+  const unsigned peers = __match_any_sync(__activemask(), word);
+  const unsigned v = __reduce_or_sync(peers, 1u << (b & 31));
+  if ((threadIdx.x & 31) == __ffs(peers) - 1) atomicOr(&bits[word], v);
+}
+
 template <class Dem>
 __device__ __forceinline__ void sweep_rays(const Dem &dem, const ShedArgs &a, int ox, int oy,
                                            unsigned *bits) {
@@ -99,19 +110,14 @@ __device__ __forceinline__ void sweep_rays(const Dem &dem, const ShedArgs &a, in
     const int omaj = my ? oy : ox, omin = my ? ox : oy;
     const int kedge = dir > 0 ? n - 1 - omaj : omaj;
     const int kend = min(dmaj * dir, kedge);
-    const int offlo = -omin, offhi = n - 1 - omin;
     const int smaj = my ? dir : dir * W, smin = my ? W : 1;
-    const float fdir = dir > 0 ? 1.f : -1.f;
-    float hs = -99999.f, fi = 0.f, fai = 0.f;
-    int moff = 0;
+    float hs = -99999.f, fai = 0.f;
     for (int k = 1; k <= kend; k++) {
-      fi = fadd(fi, fdir);  // (float)i, i = dir*k: exact
-      fai = fadd(fai, 1.f);  // (float)|i|
-      moff += smaj;
-      const int off = round_i(fmul(fi, slope));
-      if (off < offlo || off > offhi) break;
+      fai = fadd(fai, 1.f);  // (float)|i|, exact
+      const int off = round_i(fmul(dir > 0 ? fai : -fai, slope));  // round(i * slope)
+      if ((unsigned)(omin + off) >= (unsigned)n) break;
       if (k * k + off * off > roi2) break;
-      const int pelev = dem.at(obase + moff + off * smin);
+      const int pelev = dem.at(obase + k * smaj + off * smin);
       const float fa = i2f(pelev - oalt);
       // s = RN(a/|i|) can exceed hs only if a > hs*|i|; the sign of the fused
       // hs*|i| - a is exact, so the division runs only when the horizon may rise
@@ -119,18 +125,18 @@ __device__ __forceinline__ void sweep_rays(const Dem &dem, const ShedArgs &a, in
         const float s = fdiv(fa, fai);
         if (hs < s) hs = s;
       }
-      const float halt = fadd(foalt, fmul(hs, fai));
-      if (i2f(pelev + a.tht) >= halt) {
+      if (i2f(pelev + a.tht) >= fadd(foalt, fmul(hs, fai))) {
         const int i = dir * k;
-        shed_set(bits, nwpr, (my ? off : i) + roi, (my ? i : off) + roi);
+        shed_set_warp(bits, nwpr, (my ? off : i) + roi, (my ? i : off) + roi);
       }
     }
   }
 }
 
-// Two variants: CTAs of at most 800 threads capped at 40 registers per
-// thread, so two CTAs (two observers' windows) are resident per SM; and CTAs
-// of up to 1024 threads for larger roi.
+// Two variants: CTAs of at most 800 threads compiled for two resident CTAs
+// per SM (two observers' windows in flight; the per-partition register file
+// then allows 32 registers per thread), and CTAs of up to 1024 threads for
+// larger roi.
 template <bool kSmem>
 __device__ __forceinline__ void shed_body(const CUtensorMap &map, const ShedArgs &a) {
   extern __shared__ __align__(128) unsigned char sm[];
@@ -173,7 +179,7 @@ __device__ __forceinline__ void shed_body(const CUtensorMap &map, const ShedArgs
 }
 
 template <bool kSmem>
-__global__ void __maxnreg__(40)
+__global__ void __launch_bounds__(800, 2)
     shed_kernel2(const __grid_constant__ CUtensorMap map, const ShedArgs a) {
   shed_body<kSmem>(map, a);
 }
