@@ -27,6 +27,15 @@
 namespace siting {
 namespace {
 
+// Word strides of the two shed images (odd, so consecutive rows/columns fall in
+// distinct banks); the column image has 32-column padding for the transpose.
+__host__ __device__ __forceinline__ int shed_row_stride(int nr) {
+  const int w = 2 * ((nr + 63) / 64);  // reference words per row, in halves
+  return w | 1;
+}
+__host__ __device__ __forceinline__ int shed_col_stride(int nr) { return ((nr + 31) / 32) | 1; }
+__host__ __device__ __forceinline__ int shed_col_count(int nr) { return (nr + 31) / 32 * 32; }
+
 struct ShedArgs {
   const uint16_t *dem;
   int pitch, n, roi, oht, tht, nsheds;
@@ -54,29 +63,30 @@ struct GlobalDem {
   __device__ __forceinline__ int at(int o) const { return __ldg(g + o); }
 };
 
-// Sets bit (row, col) of the shed image held as 32-bit halves of 64-bit words.
-__device__ __forceinline__ void shed_set(unsigned *bits, int nwpr, int row, int col) {
-  const int w = row * nwpr + (col >> 6);
-  const int b = 63 - (col & 63);
-  atomicOr(&bits[2 * w + (b >> 5)], 1u << (b & 31));
-}
+// The shed is assembled in two shared-memory bit images.  Rays that step
+// along y put a warp's lanes on different rows at each step; they mark cells in
+// the row-major image R (word = row*rs + col/32, bit 31 - col%32, i.e. the
+// reference's MSB-first order split into 32-bit halves).  Rays that step along
+// x put the lanes on one row; they mark the column-major image C (word =
+// col*cs + row/32, bit row%32), where their words differ.  rs and cs are odd,
+// so distinct words also fall in distinct banks.  C is transposed into R at
+// the end, 32x32 bits per warp with ballots.
+struct ShedImage {
+  unsigned *R, *C;
+  int rs, cs;
+};
 
-// Same, combining the lanes that hit the same 32-bit word into one atomic: on
-// rays that step along x, a warp's lanes mark neighbouring columns of one row.
-__device__ __forceinline__ void shed_set_warp(unsigned *bits, int nwpr, int row, int col) {
-  const int w = row * nwpr + (col >> 6);
-  const int b = 63 - (col & 63);
-  const int word = 2 * w + (b >> 5);
-  const unsigned peers = __match_any_sync(__activemask(), word);
-  const unsigned v = __reduce_or_sync(peers, 1u << (b & 31));
-  if ((threadIdx.x & 31) == __ffs(peers) - 1) atomicOr(&bits[word], v);
+__device__ __forceinline__ void mark_row_major(const ShedImage &im, int row, int col) {
+  atomicOr(&im.R[row * im.rs + (col >> 5)], 1u << (31 - (col & 31)));
+}
+__device__ __forceinline__ void mark_col_major(const ShedImage &im, int row, int col) {
+  atomicOr(&im.C[col * im.cs + (row >> 5)], 1u << (row & 31));
 }
 
 template <class Dem>
 __device__ __forceinline__ void sweep_rays(const Dem &dem, const ShedArgs &a, int ox, int oy,
-                                           unsigned *bits) {
+                                           const ShedImage &im) {
   const int roi = a.roi, n = a.n, side = 2 * roi;
-  const int nwpr = (2 * roi + 1 + 63) / 64;
   const int roi2 = roi * roi;
   const int xmin = ox - roi, ymin = oy - roi, xmax = ox + roi, ymax = oy + roi;
   const int W = dem.stride();
@@ -127,7 +137,10 @@ __device__ __forceinline__ void sweep_rays(const Dem &dem, const ShedArgs &a, in
       }
       if (i2f(pelev + a.tht) >= fadd(foalt, fmul(hs, fai))) {
         const int i = dir * k;
-        shed_set_warp(bits, nwpr, (my ? off : i) + roi, (my ? i : off) + roi);
+        if (my)
+          mark_row_major(im, off + roi, i + roi);
+        else
+          mark_col_major(im, i + roi, off + roi);
       }
     }
   }
@@ -153,29 +166,57 @@ __device__ __forceinline__ void shed_body(const CUtensorMap &map, const ShedArgs
   uint16_t *win = reinterpret_cast<uint16_t *>(sm);
   const uint32_t win_bytes = kSmem ? (uint32_t)a.nboxes * a.box_rows * a.win_w * 2u : 0u;
   uint64_t *mbar = reinterpret_cast<uint64_t *>(sm + win_bytes);
-  unsigned *bits = reinterpret_cast<unsigned *>(sm + win_bytes + 16);
+  ShedImage im;
+  im.rs = shed_row_stride(nr);
+  im.cs = shed_col_stride(nr);
+  im.R = reinterpret_cast<unsigned *>(sm + win_bytes + 16);
+  im.C = im.R + nr * im.rs;
+  const int img_words = nr * im.rs + shed_col_count(nr) * im.cs;
   if (kSmem && threadIdx.x == 0) {
     mbar_init(mbar, 1);
     mbar_expect_tx(mbar, win_bytes);
     for (int b = 0; b < a.nboxes; b++)
       tma_load_2d(win + (size_t)b * a.box_rows * a.win_w, &map, hy0, hx0 + b * a.box_rows, mbar);
   }
-  for (int i = threadIdx.x; i < 2 * nwords; i += blockDim.x) bits[i] = 0u;
+  for (int i = threadIdx.x; i < img_words; i += blockDim.x) im.R[i] = 0u;
   __syncthreads();
-  if (threadIdx.x == 0) shed_set(bits, nwpr, a.roi, a.roi);  // siting.cpp:279
+  if (threadIdx.x == 0) mark_row_major(im, a.roi, a.roi);  // siting.cpp:279
   if (kSmem) {
     if (!mbar_wait(mbar, 0)) {
       if (threadIdx.x == 0) atomicOr(a.err, kErrTmaTimeout);
       return;
     }
-    sweep_rays(SmemDem{win, a.win_w, hx0, hy0}, a, ox, oy, bits);
+    sweep_rays(SmemDem{win, a.win_w, hx0, hy0}, a, ox, oy, im);
   } else {
-    sweep_rays(GlobalDem{a.dem, a.pitch}, a, ox, oy, bits);
+    sweep_rays(GlobalDem{a.dem, a.pitch}, a, ox, oy, im);
+  }
+  __syncthreads();
+  // fold C into R: one warp per 32x32 block; lane j holds column cb*32+j's
+  // bits of rows rb*32..+31, a 5-stage butterfly transpose leaves row rb*32+i
+  // in lane i (bit j = column cb*32+j), reversed into R's MSB-first order
+  const int nb32 = (nr + 31) / 32;
+  const int lane = threadIdx.x & 31;
+  for (int blk = threadIdx.x >> 5; blk < nb32 * nb32; blk += blockDim.x >> 5) {
+    const int rb = blk / nb32, cb = blk - rb * nb32;
+    unsigned x = im.C[(cb * 32 + lane) * im.cs + rb];
+    if (!__any_sync(0xffffffffu, x != 0u)) continue;
+#pragma unroll
+    for (int sh = 16; sh >= 1; sh >>= 1) {
+      const unsigned m = sh == 16 ? 0x0000FFFFu : sh == 8 ? 0x00FF00FFu : sh == 4 ? 0x0F0F0F0Fu
+                         : sh == 2 ? 0x33333333u : 0x55555555u;
+      const unsigned o = __shfl_xor_sync(0xffffffffu, x, sh);
+      x = (lane & sh) ? (x & ~m) | ((o >> sh) & m) : (x & m) | ((o << sh) & ~m);
+    }
+    const int row = rb * 32 + lane;
+    if (row < nr && x) im.R[row * im.rs + cb] |= __brev(x);
   }
   __syncthreads();
   uint64_t *dst = a.sheds + (size_t)blockIdx.x * nwords;
-  const uint64_t *src = reinterpret_cast<const uint64_t *>(bits);
-  for (int i = threadIdx.x; i < nwords; i += blockDim.x) dst[i] = src[i];
+  for (int i = threadIdx.x; i < nwords; i += blockDim.x) {
+    const int r = i / nwpr, q = i - r * nwpr;
+    const unsigned hi = im.R[r * im.rs + 2 * q], lo = im.R[r * im.rs + 2 * q + 1];
+    dst[i] = ((uint64_t)hi << 32) | lo;
+  }
 }
 
 template <bool kSmem>
@@ -208,8 +249,8 @@ WinGeom win_geom(int roi) {
 }  // namespace
 
 size_t shed_smem_bytes(const ShedPlan &p, int roi) {
-  const int nr = 2 * roi + 1, nwpr = (nr + 63) / 64;
-  size_t b = 16 + (size_t)nr * nwpr * 8;
+  const int nr = 2 * roi + 1;
+  size_t b = 16 + 4 * ((size_t)nr * shed_row_stride(nr) + (size_t)shed_col_count(nr) * shed_col_stride(nr));
   if (p.use_smem) {
     const WinGeom g = win_geom(roi);
     b += (size_t)g.nboxes * g.box_rows * g.w * 2;
