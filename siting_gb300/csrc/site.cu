@@ -63,6 +63,7 @@ struct SiteArgs {
   const int *gains;  // round-1 gains, from site_score_kernel
   int *err;
   int nslots, pick_items, pick_cap, pair_cap;
+  int ncap_words;  // shared-memory words for the round's new bits (0 = none)
   long long stop_area;  // smallest cumarea with 100.0*cumarea/n^2 > 95 (host-computed)
 };
 
@@ -172,6 +173,7 @@ __global__ void __launch_bounds__(kSiteThreads, 1) site_kernel(const SiteArgs a)
   unsigned char *s_flag = take((size_t)a.nslots);
   unsigned char *s_tag = take((size_t)a.nslots);  // bit0 touched, bit1 covered (this round)
   unsigned char *s_dirty = take((size_t)ngroups);
+  uint64_t *s_N = reinterpret_cast<uint64_t *>(take((size_t)a.ncap_words * 8));
 
   GroupBarrier gb{a.bar, (unsigned)G, 0u};
   // tracing: device cycles per phase, accumulated by CTA 0's thread 0
@@ -435,7 +437,71 @@ __global__ void __launch_bounds__(kSiteThreads, 1) site_kernel(const SiteArgs a)
     __syncthreads();
     const int npair = s_npair;
 
-    // ---- D. per (pair, row, 4-word chunk): |V_c n V_p \ cum| ----------------
+    const int nb2 = nwpr + 1;
+    const bool n_in_smem = m * nr * nb2 <= a.ncap_words;
+    if (n_in_smem) {
+      // ---- D1. new bits N = placed(p) & ~cum of each pick, in shared memory,
+      // for picks with own candidates nearby or rows of this CTA's self-check
+      for (int i = tid; i < m * nr * nb2; i += blockDim.x) {
+        const int pi = i / (nr * nb2), rem = i - pi * nr * nb2;
+        const int prow = rem / nb2, j = rem - prow * nb2;
+        const bool own_row = (prow % G) == k;
+        if (s_pcnt[pi] == 0 && !own_row) continue;
+        const int pp = s_ppos[pi];
+        const int px = pp / n, py = pp - (pp / n) * n;
+        int fwp, fbp;
+        shed_align(py - roi, fwp, fbp);
+        const int gr = px - roi + prow, W = fwp + j;
+        uint64_t v = 0;
+        if (gr >= 0 && gr < n && W >= 0 && W < cw)
+          v = placed_word(a.sheds + (size_t)s_pk[pi] * per + (size_t)prow * nwpr, j, nwpr, fbp) &
+              ~__ldcg(cum + (size_t)gr * cw + W);
+        s_N[i] = v;
+        if (own_row && v) atomicAdd(a.ncount + par * kMaxPicks + pi, __popcll(v));
+      }
+      __syncthreads();
+      // ---- D2. per (pair, row, 4-word chunk): popcount(placed(c) & N) ------
+      for (int i = tid; i < npair * nr * nch; i += blockDim.x) {
+        const int u = i / (nr * nch), rem = i - u * nr * nch;
+        const int pr = s_plist[u];
+        const int pi = pr / pcap;
+        const int r = rem / nch, ch = rem - r * nch;
+        const int s = s_pairslot[pr];
+        const int cp = s_pos[s], pp = s_ppos[pi];
+        const int cx = cp / n, cy = cp - cx * n, px = pp / n, py = pp - px * n;
+        const int gr = cx - roi + r, prow = gr - (px - roi);
+        if (prow < 0 || prow >= nr || gr < 0 || gr >= n) continue;
+        int fwc, fbc, fwp, fbp;
+        shed_align(cy - roi, fwc, fbc);
+        shed_align(py - roi, fwp, fbp);
+        const uint64_t *nrow = s_N + (size_t)(pi * nr + prow) * nb2;
+        if (a.intervis && r == roi && ch == 0) {  // own cell: newly covered by the pick?
+          const int j = (cy >> 6) - fwp;
+          if (j >= 0 && j < nb2 && ((nrow[j] >> (63 - (cy & 63))) & 1ull))
+            atomicOr(reinterpret_cast<unsigned *>(s_paircov + (pr & ~3)), 1u << (8 * (pr & 3)));
+        }
+        const int lwc = (cy + roi) >> 6;
+        const int lo = max(max(fwc, fwp), 0), hi = min(min(lwc, fwp + nwpr), cw - 1);
+        const int W0 = lo + 4 * ch;
+        if (W0 > hi) continue;
+        const uint64_t *crow = a.sheds + (size_t)(s * G + k) * per + (size_t)r * nwpr;
+        uint64_t cwd[5];
+#pragma unroll
+        for (int q = 0; q < 5; q++) {
+          const int jc = W0 - fwc - 1 + q;
+          cwd[q] = (jc >= 0 && jc < nwpr) ? __ldg(crow + jc) : 0ull;
+        }
+        int d = 0;
+#pragma unroll
+        for (int q = 0; q < 4; q++) {
+          if (W0 + q > hi) break;
+          const uint64_t vc = (cwd[q + 1] >> fbc) | (fbc ? cwd[q] << (64 - fbc) : 0ull);
+          d += __popcll(vc & nrow[W0 + q - fwp]);
+        }
+        if (d) atomicAdd(&s_pairdelta[pr], d);
+      }
+    } else {
+      // ---- D. (fallback) per (pair, row, 4-word chunk): |V_c n V_p \ cum| --
     // Every load of an item is independent (pair cell, pick cell, three rows),
     // so an item costs one memory latency.  Rows outside the overlap of the
     // two windows are skipped.
@@ -503,6 +569,7 @@ __global__ void __launch_bounds__(kSiteThreads, 1) site_kernel(const SiteArgs a)
             ~__ldcg(cum + (size_t)gr * cw + W);
         if (v) atomicAdd(a.ncount + par * kMaxPicks + pi, __popcll(v));
       }
+    }
     }
     __syncthreads();
     mark(4);
@@ -761,7 +828,10 @@ int site_default_ctas(int nsheds, int sm_count) {
   return std::min(g, std::min(sm_count, 160));
 }
 
-size_t site_smem_bytes(int roi, int nsheds, int nctas, int nblocks, int npb, float blocksize) {
+namespace {
+
+// Shared memory of everything but the new-bits buffer.
+size_t site_smem_base(int roi, int nsheds, int nctas, int nblocks, int npb, float blocksize) {
   const int nslots = (nsheds + nctas - 1) / nctas;
   const int ngroups = (nslots + 31) / 32;
   const int GK = nctas * kTopK;
@@ -774,6 +844,21 @@ size_t site_smem_bytes(int roi, int nsheds, int nctas, int nblocks, int npb, flo
   b += 3 * round16((size_t)pair_cap * 4) + round16((size_t)pair_cap);
   b += 2 * round16((size_t)nslots) + round16((size_t)ngroups);
   return b;
+}
+
+constexpr size_t kSiteSmemPlan = 220 * 1024;
+constexpr int kMaxNWords = 16384;  // 128 KB of new bits: ~16 picks at roi=100
+
+int site_ncap_words(size_t base) {
+  if (base >= kSiteSmemPlan) return 0;
+  return (int)std::min<size_t>(kMaxNWords, (kSiteSmemPlan - base) / 8 / 2 * 2);
+}
+
+}  // namespace
+
+size_t site_smem_bytes(int roi, int nsheds, int nctas, int nblocks, int npb, float blocksize) {
+  const size_t base = site_smem_base(roi, nsheds, nctas, nblocks, npb, blocksize);
+  return base + round16((size_t)site_ncap_words(base) * 8);
 }
 
 bool site_supported(int roi, int nsheds, int nctas) {
@@ -811,6 +896,7 @@ cudaError_t launch_site(int nrows, int roi, int intervis, int nsheds, const int3
   a.pick_items = pb.items;
   a.pick_cap = pb.cap;
   a.pair_cap = site_pair_cap(pb);
+  a.ncap_words = site_ncap_words(site_smem_base(roi, nsheds, nctas, nblocks, npb, blocksize));
   a.stop_area = site_stop_area(nrows);
   const size_t shm = site_smem_bytes(roi, nsheds, nctas, nblocks, npb, blocksize);
   const int nr = 2 * roi + 1, per = nr * ((nr + 63) / 64);
