@@ -151,9 +151,10 @@ int siting_site_it_dev(siting_ctx *ctx, int nrows, int roi, int intervis,
 int siting_last_pick_order(siting_ctx *ctx, int32_t *order, int cap, int *count);
 
 /* Tracing: device clock cycles CTA 0 spent in each phase of the last SITE
- * run (0 initial scores, 1 max-tree refresh + publish, 2 group barrier,
- * 3 agreeing on the pick, 4 new bits + neighbour search, 5 gain deltas,
- * 6 intervis gate and updates).  Writes min(n, 7) values. */
+ * run, summed over rounds: 0 set-up, 1 publishing its top keys, 2 round
+ * barrier, 3 merging the lists and choosing the round's picks, 4 finding the
+ * candidates near the picks, 5 compacting them, 6 gain deltas, 7 intervis cut
+ * and second barrier, 8 applying the picks.  Writes min(n, 9) values. */
 int siting_last_site_phase_cycles(siting_ctx *ctx, long long *cycles, int n);
 
 /* SITE on device buffers without allocating any memory.  No counterpart in

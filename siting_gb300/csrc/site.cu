@@ -177,7 +177,7 @@ __global__ void __launch_bounds__(kSiteThreads, 1) site_kernel(const SiteArgs a)
 
   GroupBarrier gb{a.bar, (unsigned)G, 0u};
   // tracing: device cycles per phase, accumulated by CTA 0's thread 0
-  long long ph[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+  long long ph[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
   long long tmark = clock64();
   auto mark = [&](int i) {
     if (k == 0 && tid == 0) {
@@ -409,6 +409,7 @@ __global__ void __launch_bounds__(kSiteThreads, 1) site_kernel(const SiteArgs a)
       }
     }
     __syncthreads();
+    mark(4);
 
     // compact the pairs: offsets of each pick's pairs, then a dense index list
     if (warp == 0) {
@@ -436,6 +437,7 @@ __global__ void __launch_bounds__(kSiteThreads, 1) site_kernel(const SiteArgs a)
     }
     __syncthreads();
     const int npair = s_npair;
+    mark(5);
 
     const int nb2 = nwpr + 1;
     const bool n_in_smem = m * nr * nb2 <= a.ncap_words;
@@ -572,7 +574,7 @@ __global__ void __launch_bounds__(kSiteThreads, 1) site_kernel(const SiteArgs a)
     }
     }
     __syncthreads();
-    mark(4);
+    mark(6);
 
     // ---- E. intervis: where would a newly covered candidate overtake? --------
     if (tid == 0) s_roundcut = m;
@@ -645,7 +647,7 @@ __global__ void __launch_bounds__(kSiteThreads, 1) site_kernel(const SiteArgs a)
     }
     __syncthreads();
     const int mcut = s_mcut;
-    mark(5);
+    mark(7);
 
     // ---- F. apply picks 0..mcut-1 -------------------------------------------
     if (k == 0 && tid >= blockDim.x - kMaxPicks) {  // self-check this round, then reset
@@ -717,7 +719,7 @@ __global__ void __launch_bounds__(kSiteThreads, 1) site_kernel(const SiteArgs a)
       s_done = (s_stop_at > 0 && s_stop_at <= mcut) ? 1 : 0;
     }
     __syncthreads();
-    mark(6);
+    mark(8);
     npicks += mcut;
     nprev = mcut;
     rounds++;
@@ -728,7 +730,7 @@ __global__ void __launch_bounds__(kSiteThreads, 1) site_kernel(const SiteArgs a)
     a.out[0] = npicks;
     a.out[1] = s_cum;
     a.out[2] = rounds;
-    for (int i = 0; i < 7; i++) a.out[3 + i] = ph[i];
+    for (int i = 0; i < 9; i++) a.out[3 + i] = ph[i];
   }
 }
 
