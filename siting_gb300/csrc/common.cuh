@@ -85,6 +85,15 @@ __device__ __forceinline__ void tma_load_2d(void *dst, const CUtensorMap *map, i
       : "memory");
 }
 
+// Bulk prefetch of [p, p+bytes) into L2 (p and bytes rounded out to 16 bytes).
+__device__ __forceinline__ void prefetch_l2(const void *p, size_t bytes) {
+  const uintptr_t a = reinterpret_cast<uintptr_t>(p) & ~uintptr_t(15);
+  const uintptr_t e = (reinterpret_cast<uintptr_t>(p) + bytes + 15) & ~uintptr_t(15);
+  if (e > a)
+    asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(a), "r"((unsigned)(e - a))
+                 : "memory");
+}
+
 // ---- bounded barrier over a group of co-resident CTAs ------------------------
 // bar[0] counts arrivals and is never reset: the g-th barrier completes when
 // it reaches g * nctas.  One release-add per CTA, then acquire-polls.  Must be

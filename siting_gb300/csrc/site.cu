@@ -133,9 +133,12 @@ __global__ void __launch_bounds__(256) site_score_kernel(const uint64_t *sheds, 
 
 __global__ void __launch_bounds__(kSiteThreads, 1) site_kernel(const SiteArgs a) {
   extern __shared__ __align__(16) unsigned char sm[];
-  __shared__ int s_m, s_mcut, s_stop_at, s_done, s_flagv, s_roundcut, s_npair;
+  __shared__ int s_m, s_mcut, s_stop_at, s_done, s_flagv, s_roundcut, s_npair, s_nvalid;
   __shared__ long long s_cum;
   __shared__ int s_poff[kMaxPicks + 1];
+  __shared__ unsigned long long s_red[32];
+  __shared__ int s_rank[kMaxPicks];
+  __shared__ unsigned char s_near[kMaxPicks];
 
   const int G = a.G, k = blockIdx.x;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nwarps = blockDim.x >> 5;
@@ -163,6 +166,8 @@ __global__ void __launch_bounds__(kSiteThreads, 1) site_kernel(const SiteArgs a)
   int *s_pos = reinterpret_cast<int *>(take((size_t)a.nslots * 4));
   int *s_dacc = reinterpret_cast<int *>(take((size_t)a.nslots * 4));
   int *s_mpos = reinterpret_cast<int *>(take((size_t)GK * 4));
+  int *s_valid = reinterpret_cast<int *>(take((size_t)GK * 4));
+  int *s_vrank = reinterpret_cast<int *>(take((size_t)GK * 4));
   int *s_pk = reinterpret_cast<int *>(take(kMaxPicks * 4));    // pick: candidate index
   int *s_ppos = reinterpret_cast<int *>(take(kMaxPicks * 4));  // pick: cell
   int *s_pcnt = reinterpret_cast<int *>(take(kMaxPicks * 4));  // own candidates near the pick
@@ -283,81 +288,92 @@ __global__ void __launch_bounds__(kSiteThreads, 1) site_kernel(const SiteArgs a)
       s_mpos[i] = (int)__ldcg(src + 1);
     }
     if (tid < kMaxPicks) s_pcnt[tid] = 0;
+    if (tid == 0) s_nvalid = 0;
     __syncthreads();
-    if (warp == 0) {
-      // exactness threshold: unpublished keys are below each full list's last key
+    {  // exactness threshold: unpublished keys are below each full list's last key
       unsigned long long T = 0;
-      for (int g = lane; g < G; g += 32) {
-        const unsigned long long last = s_mkey[g * kTopK + kTopK - 1];
-        T = last > T ? last : T;
-      }
+      if (tid < G) T = s_mkey[tid * kTopK + kTopK - 1];
 #pragma unroll
       for (int o = 16; o > 0; o >>= 1) {
         const unsigned long long w = __shfl_xor_sync(0xffffffffu, T, o);
         T = w > T ? w : T;
       }
-      int h0 = 0, h1 = 0, h2 = 0, h3 = 0, h4 = 0;  // heads of lists lane+32q
+      if (lane == 0 && warp * 32 < G) s_red[warp] = T;
+    }
+    __syncthreads();
+    {
+      unsigned long long T = 0;
+      for (int w = 0; w * 32 < G; w++) T = s_red[w] > T ? s_red[w] : T;
+      // exactly ordered entries: keys >= T with a positive area
+      for (int e = tid; e < GK; e += blockDim.x) {
+        const unsigned long long key = s_mkey[e];
+        if (key == 0 || (key >> 32) == 0 || key < T) continue;
+        const int v = atomicAdd(&s_nvalid, 1);
+        s_valid[v] = e;  // GK entries fit
+        s_vrank[v] = 0;
+      }
+    }
+    __syncthreads();
+    const int nvalid = s_nvalid;
+    {  // rank of each valid key: count larger valid keys, 32 at a time
+      const int nch = (nvalid + 31) / 32;
+      for (int i = tid; i < nvalid * nch; i += blockDim.x) {
+        const int v = i / nch, c0 = (i - v * nch) * 32;
+        const unsigned long long key = s_mkey[s_valid[v]];
+        int cnt = 0;
+        for (int j = c0; j < min(c0 + 32, nvalid); j++) cnt += s_mkey[s_valid[j]] > key;
+        if (cnt) atomicAdd(&s_vrank[v], cnt);
+      }
+    }
+    __syncthreads();
+    for (int v = tid; v < nvalid; v += blockDim.x)
+      if (s_vrank[v] < kMaxPicks) s_rank[s_vrank[v]] = s_valid[v];
+    __syncthreads();
+    const int nrank = min(nvalid, kMaxPicks);
+    if (tid < nrank) {  // usable if > 2roi from every better-ranked entry
+      const int pos = s_mpos[s_rank[tid]];
+      const int px = pos / n, py = pos - (pos / n) * n;
+      bool near = false;
+      for (int j = 0; j < tid; j++) {
+        const int q = s_mpos[s_rank[j]];
+        const int dx = q / n - px, dy = q - (q / n) * n - py;
+        near |= dx * dx + dy * dy <= lim2;
+      }
+      s_near[tid] = near;
+    }
+    __syncthreads();
+    if (warp == 0) {  // prefix: leading usable ranks, capped, up to the 95% stop
+      const int max_m = min(kMaxPicks, a.pair_cap / max(pcap, 1));
       long long cumv = s_cum;
       int m = 0, stop_at = -1;
-      const int max_m = min(kMaxPicks, a.pair_cap / max(pcap, 1));
-      while (m < max_m) {
-        unsigned long long key = 0;
-        int idx = -1;
+      for (int base = 0; base < nrank && base < max_m; base += 32) {
+        const int r = base + lane;
+        const bool ok = r < nrank && r < max_m && !s_near[r];
+        const unsigned okm = __ballot_sync(0xffffffffu, ok);
+        const int run = okm == 0xffffffffu ? 32 : __ffs(~okm) - 1;
+        long long v = lane < run ? (long long)(s_mkey[s_rank[r]] >> 32) : 0;
 #pragma unroll
-        for (int q = 0; q < 5; q++) {
-          const int g = lane + 32 * q;
-          const int h = q == 0 ? h0 : q == 1 ? h1 : q == 2 ? h2 : q == 3 ? h3 : h4;
-          if (g < G && h < kTopK) {
-            const int e = g * kTopK + h;
-            const unsigned long long v = s_mkey[e];
-            if (v > key) {
-              key = v;
-              idx = e;
-            }
-          }
+        for (int o = 1; o < 32; o <<= 1) {
+          const long long w = __shfl_up_sync(0xffffffffu, v, o);
+          if (lane >= o) v += w;
         }
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) {
-          const unsigned long long w = __shfl_xor_sync(0xffffffffu, key, o);
-          const int e2 = __shfl_xor_sync(0xffffffffu, idx, o);
-          if (w > key) {
-            key = w;
-            idx = e2;
-          }
-        }
-        if (key == 0 || (key >> 32) == 0 || key < T) break;
-        const int pos = s_mpos[idx];
-        const int px = pos / n, py = pos - (pos / n) * n;
-        bool near = false;
-        for (int j = lane; j < m; j += 32) {
-          const int q = s_ppos[j];
-          const int dx = q / n - px, dy = q - (q / n) * n - py;
-          near |= dx * dx + dy * dy <= lim2;
-        }
-        if (__any_sync(0xffffffffu, near)) break;
-        if (lane == 0) {
-          s_pk[m] = key_index(key);
-          s_ppos[m] = pos;
-          s_pkey[m] = key;
-        }
-        {
-          const int g = idx / kTopK;
-          if (lane == (g & 31)) {
-            const int q = g >> 5;
-            h0 += q == 0;
-            h1 += q == 1;
-            h2 += q == 2;
-            h3 += q == 3;
-            h4 += q == 4;
-          }
-        }
-        __syncwarp();
-        cumv += (long long)(key >> 32);
-        m++;
-        if (cumv >= a.stop_area) {
-          stop_at = m;  // the reference stops after this pick
+        const unsigned hit = __ballot_sync(0xffffffffu, lane < run && cumv + v >= a.stop_area);
+        if (hit) {
+          m = base + __ffs(hit);
+          stop_at = m;
           break;
         }
+        m = base + run;
+        cumv += __shfl_sync(0xffffffffu, v, 31);
+        if (run < 32) break;
+      }
+      for (int j = lane; j < m; j += 32) {
+        const int e = s_rank[j];
+        const int c = key_index(s_mkey[e]);
+        s_pk[j] = c;
+        s_ppos[j] = s_mpos[e];
+        s_pkey[j] = s_mkey[e];
+        prefetch_l2(a.sheds + (size_t)c * per, per * 8);  // the pick's shed, for D1
       }
       if (lane == 0) {
         s_m = m;
@@ -396,6 +412,12 @@ __global__ void __launch_bounds__(kSiteThreads, 1) site_kernel(const SiteArgs a)
         const int idx = atomicAdd(&s_pcnt[pi], 1);
         if (idx < pcap) {
           const int pr = pi * pcap + idx;
+          {  // rows of c's shed that overlap the pick's window, for the deltas
+            const int r0 = max(0, px - cx), r1 = min(nr - 1, px - cx + 2 * roi);
+            if (r1 >= r0)
+              prefetch_l2(a.sheds + (size_t)c * per + (size_t)r0 * nwpr,
+                          (size_t)(r1 - r0 + 1) * nwpr * 8);
+          }
           s_pairslot[pr] = s;
           s_pairdelta[pr] = 0;
           unsigned char cv = 0;
@@ -441,33 +463,49 @@ __global__ void __launch_bounds__(kSiteThreads, 1) site_kernel(const SiteArgs a)
 
     const int nb2 = nwpr + 1;
     const bool n_in_smem = m * nr * nb2 <= a.ncap_words;
-    if (n_in_smem) {
-      // ---- D1. new bits N = placed(p) & ~cum of each pick, in shared memory,
-      // for picks with own candidates nearby or rows of this CTA's self-check
-      for (int i = tid; i < m * nr * nb2; i += blockDim.x) {
-        const int pi = i / (nr * nb2), rem = i - pi * nr * nb2;
-        const int prow = rem / nb2, j = rem - prow * nb2;
+    if (n_in_smem && nwpr <= 7) {
+      // ---- D1. new bits N = placed(p) & ~cum of each pick row, in shared
+      // memory (picks with own candidates nearby, or rows of this CTA's
+      // self-check); one item per row, all of its loads issued together
+      for (int it = tid; it < m * nr; it += blockDim.x) {
+        const int pi = it / nr, prow = it - pi * nr;
         const bool own_row = (prow % G) == k;
         if (s_pcnt[pi] == 0 && !own_row) continue;
         const int pp = s_ppos[pi];
         const int px = pp / n, py = pp - (pp / n) * n;
         int fwp, fbp;
         shed_align(py - roi, fwp, fbp);
-        const int gr = px - roi + prow, W = fwp + j;
-        uint64_t v = 0;
-        if (gr >= 0 && gr < n && W >= 0 && W < cw)
-          v = placed_word(a.sheds + (size_t)s_pk[pi] * per + (size_t)prow * nwpr, j, nwpr, fbp) &
-              ~__ldcg(cum + (size_t)gr * cw + W);
-        s_N[i] = v;
-        if (own_row && v) atomicAdd(a.ncount + par * kMaxPicks + pi, __popcll(v));
+        const int gr = px - roi + prow;
+        uint64_t *nrow = s_N + (size_t)it * nb2;
+        if (gr < 0 || gr >= n) {
+          for (int j = 0; j < nb2; j++) nrow[j] = 0ull;
+          continue;
+        }
+        const uint64_t *prw = a.sheds + (size_t)s_pk[pi] * per + (size_t)prow * nwpr;
+        const uint64_t *xr = cum + (size_t)gr * cw;
+        uint64_t w[8], x[8];
+#pragma unroll
+        for (int q = 0; q < 8; q++) {
+          w[q] = q < nwpr ? __ldg(prw + q) : 0ull;
+          const int W = fwp + q;
+          x[q] = (q < nb2 && W >= 0 && W < cw) ? __ldcg(xr + W) : ~0ull;
+        }
+        int cnt = 0;
+#pragma unroll
+        for (int q = 0; q < 8; q++) {
+          if (q >= nb2) break;
+          const uint64_t v = ((w[q] >> fbp) | ((q > 0 && fbp) ? w[q - 1] << (64 - fbp) : 0ull)) & ~x[q];
+          nrow[q] = v;
+          cnt += __popcll(v);
+        }
+        if (own_row && cnt) atomicAdd(a.ncount + par * kMaxPicks + pi, cnt);
       }
       __syncthreads();
-      // ---- D2. per (pair, row, 4-word chunk): popcount(placed(c) & N) ------
-      for (int i = tid; i < npair * nr * nch; i += blockDim.x) {
-        const int u = i / (nr * nch), rem = i - u * nr * nch;
+      // ---- D2. per (pair, row): popcount(placed(c) & N) ----------------------
+      for (int it = tid; it < npair * nr; it += blockDim.x) {
+        const int u = it / nr, r = it - u * nr;
         const int pr = s_plist[u];
         const int pi = pr / pcap;
-        const int r = rem / nch, ch = rem - r * nch;
         const int s = s_pairslot[pr];
         const int cp = s_pos[s], pp = s_ppos[pi];
         const int cx = cp / n, cy = cp - cx * n, px = pp / n, py = pp - px * n;
@@ -477,28 +515,26 @@ __global__ void __launch_bounds__(kSiteThreads, 1) site_kernel(const SiteArgs a)
         shed_align(cy - roi, fwc, fbc);
         shed_align(py - roi, fwp, fbp);
         const uint64_t *nrow = s_N + (size_t)(pi * nr + prow) * nb2;
-        if (a.intervis && r == roi && ch == 0) {  // own cell: newly covered by the pick?
+        if (a.intervis && r == roi) {  // own cell: newly covered by the pick?
           const int j = (cy >> 6) - fwp;
           if (j >= 0 && j < nb2 && ((nrow[j] >> (63 - (cy & 63))) & 1ull))
             atomicOr(reinterpret_cast<unsigned *>(s_paircov + (pr & ~3)), 1u << (8 * (pr & 3)));
         }
-        const int lwc = (cy + roi) >> 6;
-        const int lo = max(max(fwc, fwp), 0), hi = min(min(lwc, fwp + nwpr), cw - 1);
-        const int W0 = lo + 4 * ch;
-        if (W0 > hi) continue;
+        const int lo = max(max(fwc, fwp), 0);
+        const int hi = min(min((cy + roi) >> 6, fwp + nwpr), cw - 1);
+        if (lo > hi) continue;
         const uint64_t *crow = a.sheds + (size_t)(s * G + k) * per + (size_t)r * nwpr;
-        uint64_t cwd[5];
+        uint64_t w[8];
 #pragma unroll
-        for (int q = 0; q < 5; q++) {
-          const int jc = W0 - fwc - 1 + q;
-          cwd[q] = (jc >= 0 && jc < nwpr) ? __ldg(crow + jc) : 0ull;
-        }
+        for (int q = 0; q < 8; q++) w[q] = q < nwpr ? __ldg(crow + q) : 0ull;
         int d = 0;
 #pragma unroll
-        for (int q = 0; q < 4; q++) {
-          if (W0 + q > hi) break;
-          const uint64_t vc = (cwd[q + 1] >> fbc) | (fbc ? cwd[q] << (64 - fbc) : 0ull);
-          d += __popcll(vc & nrow[W0 + q - fwp]);
+        for (int q = 0; q < 8; q++) {  // c's placed word q lands at column word fwc+q
+          if (q >= nb2) break;
+          const int W = fwc + q;
+          if (W < lo || W > hi) continue;
+          const uint64_t vc = (w[q] >> fbc) | ((q > 0 && fbc) ? w[q - 1] << (64 - fbc) : 0ull);
+          d += __popcll(vc & nrow[W - fwp]);
         }
         if (d) atomicAdd(&s_pairdelta[pr], d);
       }
@@ -842,7 +878,7 @@ size_t site_smem_base(int roi, int nsheds, int nctas, int nblocks, int npb, floa
   size_t b = 0;
   b += round16((size_t)ngroups * kTopK * 8) + round16((size_t)GK * 8) + round16(kMaxPicks * 8);
   b += 4 * round16((size_t)nslots * 4);
-  b += round16((size_t)GK * 4) + 3 * round16(kMaxPicks * 4);
+  b += 3 * round16((size_t)GK * 4) + 3 * round16(kMaxPicks * 4);
   b += 3 * round16((size_t)pair_cap * 4) + round16((size_t)pair_cap);
   b += 2 * round16((size_t)nslots) + round16((size_t)ngroups);
   return b;
