@@ -167,6 +167,7 @@ __global__ void __launch_bounds__(kSiteThreads, 1) site_kernel(const SiteArgs a)
   int *s_dacc = reinterpret_cast<int *>(take((size_t)a.nslots * 4));
   int *s_mpos = reinterpret_cast<int *>(take((size_t)GK * 4));
   int *s_valid = reinterpret_cast<int *>(take((size_t)GK * 4));
+  unsigned long long *s_vkey = reinterpret_cast<unsigned long long *>(take((size_t)GK * 8));
   int *s_vrank = reinterpret_cast<int *>(take((size_t)GK * 4));
   int *s_pk = reinterpret_cast<int *>(take(kMaxPicks * 4));    // pick: candidate index
   int *s_ppos = reinterpret_cast<int *>(take(kMaxPicks * 4));  // pick: cell
@@ -310,6 +311,7 @@ __global__ void __launch_bounds__(kSiteThreads, 1) site_kernel(const SiteArgs a)
         if (key == 0 || (key >> 32) == 0 || key < T) continue;
         const int v = atomicAdd(&s_nvalid, 1);
         s_valid[v] = e;  // GK entries fit
+        s_vkey[v] = key;
         s_vrank[v] = 0;
       }
     }
@@ -319,9 +321,11 @@ __global__ void __launch_bounds__(kSiteThreads, 1) site_kernel(const SiteArgs a)
       const int nch = (nvalid + 31) / 32;
       for (int i = tid; i < nvalid * nch; i += blockDim.x) {
         const int v = i / nch, c0 = (i - v * nch) * 32;
-        const unsigned long long key = s_mkey[s_valid[v]];
+        const unsigned long long key = s_vkey[v];
+        const int c1 = min(c0 + 32, nvalid);
         int cnt = 0;
-        for (int j = c0; j < min(c0 + 32, nvalid); j++) cnt += s_mkey[s_valid[j]] > key;
+#pragma unroll 8
+        for (int j = c0; j < c1; j++) cnt += s_vkey[j] > key;
         if (cnt) atomicAdd(&s_vrank[v], cnt);
       }
     }
@@ -878,7 +882,7 @@ size_t site_smem_base(int roi, int nsheds, int nctas, int nblocks, int npb, floa
   size_t b = 0;
   b += round16((size_t)ngroups * kTopK * 8) + round16((size_t)GK * 8) + round16(kMaxPicks * 8);
   b += 4 * round16((size_t)nslots * 4);
-  b += 3 * round16((size_t)GK * 4) + 3 * round16(kMaxPicks * 4);
+  b += 3 * round16((size_t)GK * 4) + round16((size_t)GK * 8) + 3 * round16(kMaxPicks * 4);
   b += 3 * round16((size_t)pair_cap * 4) + round16((size_t)pair_cap);
   b += 2 * round16((size_t)nslots) + round16((size_t)ngroups);
   return b;
