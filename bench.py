@@ -44,6 +44,24 @@ WORKLOADS = {
 }
 METRIC = "DEM cells/s end-to-end"
 
+# The batched workload: 64 DEMs, sides log-uniform in [512, 2048] rounded to a
+# multiple of 32, amplitude U[2000, 30000], roi U[25, 150], height U[20, 300],
+# targets in {32, 64, 128}, bw in {8, 16, 32}, nwanted = cells/64, intervis
+# alternating, one seed per DEM.
+def batch_jobs(njobs=64, seed=64, lo=512, hi=2048):
+    import siting_gb300 as sg
+
+    rng = np.random.default_rng(seed)
+    jobs = []
+    for j in range(njobs):
+        n = int(round(np.exp(rng.uniform(np.log(lo), np.log(hi))) / 32)) * 32
+        amp = int(rng.integers(2000, 30001))
+        p = sg.Params(nrows=n, roi=int(rng.integers(25, 151)), height=int(rng.integers(20, 301)),
+                      ntests=int(rng.choice([32, 64, 128])), bw=int(rng.choice([8, 16, 32])),
+                      nwanted0=n * n // 64, intervis=j % 2)
+        jobs.append((p, dict(seed=seed * 1000 + j, range_max=amp)))
+    return jobs
+
 
 def make_dem(w, seed_offset=0):
     import siting_gb300 as sg
@@ -320,20 +338,85 @@ def run_reference(args, w):
                       f"nwanted scaled to {nw}; whole pipeline"}
 
 
+def run_batch_workload(args):
+    """Batched form vs one plain job after another, same GPU, same inputs."""
+    import torch
+
+    import siting_gb300 as sg
+
+    torch.cuda.set_device(0)
+    jobs = batch_jobs(args.batch_jobs)
+    params = [p for p, _ in jobs]
+    dems = [sg.fbm_dem(p.nrows, d["seed"], octaves=8, range_max=d["range_max"]) for p, d in jobs]
+    geos = [sg.block_geometry(p.nrows, p.bw, p.nwanted0) for p in params]
+    cells = sum(p.nrows ** 2 for p in params)
+    d_dems = [torch.from_numpy(d.view(np.int16)).cuda() for d in dems]
+    obs_b = [torch.empty(g.nwanted, dtype=torch.int32, device="cuda") for g in geos]
+    sel_b = [torch.empty(g.nwanted, dtype=torch.uint8, device="cuda") for g in geos]
+    obs_p = [torch.empty(g.nwanted, dtype=torch.int32, device="cuda") for g in geos]
+    sel_p = [torch.empty(g.nwanted, dtype=torch.uint8, device="cuda") for g in geos]
+    cb, cp = sg.Context(0), sg.Context(0)
+    sb, spl = torch.cuda.ExternalStream(cb.stream), torch.cuda.ExternalStream(cp.stream)
+    flush = torch.empty(512 << 20, dtype=torch.uint8, device="cuda")
+
+    def timed(stream, fn):
+        flush.zero_()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        r = fn()
+        e1.record(stream)
+        e1.synchronize()
+        return e0.elapsed_time(e1), r
+
+    batched = lambda: cb.run_batch_dev(params, d_dems, obs_b, sel_b)  # noqa: E731
+    plain = lambda: [cp.run_dev(p, d, o, s) for p, d, o, s in zip(params, d_dems, obs_p, sel_p)]  # noqa: E731
+    for _ in range(args.warmup):
+        timed(sb, batched)
+        timed(spl, plain)
+    tb = [timed(sb, batched)[0] for _ in range(args.steps)]
+    tp = [timed(spl, plain)[0] for _ in range(args.steps)]
+    rb = batched()
+    rp = plain()
+    torch.cuda.synchronize()
+    same = all(torch.equal(a, b) for a, b in zip(obs_b, obs_p)) and \
+        all(torch.equal(a, b) for a, b in zip(sel_b, sel_p)) and \
+        all((x.nusedsheds, x.cumarea) == (y.nusedsheds, y.cumarea) for x, y in zip(rb, rp))
+    mb, mp = sum(tb) / len(tb), sum(tp) / len(tp)
+    out = {"metric": METRIC + " (batched)", "value": cells / (mb / 1e3), "unit": "cells/s",
+           "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": mb,
+           "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32/u64",
+           "data": "synthetic",
+           "config": {"workload": f"batch{len(jobs)}_512_2048", "jobs": len(jobs), "cells": cells,
+                      "l2": "flushed (512 MiB write) between steps"},
+           "plain": {"value": cells / (mp / 1e3), "unit": "cells/s", "ms_per_step": mp},
+           "speedup_vs_plain": mp / mb, "bit_identical_to_plain": bool(same),
+           "batch_phase_ms": {"upload": rb[0].ms_h2d, "vix": rb[0].ms_vix,
+                              "findmax": rb[0].ms_findmax, "viewshed": rb[0].ms_viewshed,
+                              "site": rb[0].ms_site},
+           "site_rounds_max": max(r.site_rounds for r in rb)}
+    print(json.dumps(out))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--workload", default="c2_4096", choices=sorted(WORKLOADS))
+    ap.add_argument("--workload", default="c2_4096", choices=sorted(WORKLOADS) + ["c3_batch"])
     ap.add_argument("--cpu-sample-rows", type=int, default=2048)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--batch-jobs", type=int, default=64)
     ap.add_argument("--site-ctas", type=int, default=0,
                     help="CTAs of the SITE kernel (0 = library default)")
     args = ap.parse_args()
-    w = WORKLOADS[args.workload]
     rank = int(os.environ.get("RANK", "0"))
+    if args.workload == "c3_batch":
+        if args.impl == "gb300" and rank == 0:
+            run_batch_workload(args)
+        return
+    w = WORKLOADS[args.workload]
 
     if args.impl == "reference":
         if rank != 0:

@@ -62,6 +62,15 @@ typedef struct siting_geometry {
   int nwanted;
 } siting_geometry;
 
+/* Launch plan of one job (tile shapes and CTA counts); 0 / -1 fields take
+ * the library default.  Results never depend on the plan. */
+typedef struct siting_plan {
+  int vix_tile;     /* VIX cell tile side: 16, 32 or 64 (0 = default) */
+  int vix_smem;     /* 1: stage the DEM halo by TMA, 0: read through L1, -1: default */
+  int shed_smem;    /* 1: stage the observer window by TMA, 0: L1, -1: default */
+  int site_ctas;    /* CTAs of the job's SITE group (0 = default) */
+} siting_plan;
+
 /* Outcome and per-stage device times of one job. */
 typedef struct siting_result {
   int nusedsheds;    /* observers selected (siting.cpp:617) */
@@ -184,6 +193,24 @@ int siting_run(siting_ctx *ctx, const siting_params *p, const uint16_t *elevs,
 int siting_run_dev(siting_ctx *ctx, const siting_params *p,
                    const uint16_t *d_elevs, int32_t *d_obs,
                    uint8_t *d_selected, siting_result *res);
+
+/* ---- batched form --------------------------------------------------------
+ * Runs `njobs` independent jobs (DEMs of any sizes and parameters) as one
+ * batch: every job's VIX, FINDMAX and VIEWSHED kernels are enqueued back to
+ * back on the context's stream, then the greedy SITE selections of many jobs
+ * run concurrently in shared cooperative launches (each job's CTA group with
+ * its own barrier and scratch).  elevs[j] is job j's row-major uint16 DEM on
+ * the host; obs[j] and selected[j] receive nwanted entries.  plans may be
+ * NULL.  Each job's results equal siting_run's on the same input. */
+int siting_run_batch(siting_ctx *ctx, int njobs, const siting_params *params,
+                     const uint16_t *const *elevs, int32_t *const *obs,
+                     uint8_t *const *selected, siting_result *results,
+                     const siting_plan *plans);
+/* Device-resident form: DEMs, observers and selections in device memory. */
+int siting_run_batch_dev(siting_ctx *ctx, int njobs, const siting_params *params,
+                         const uint16_t *const *d_elevs, int32_t *const *d_obs,
+                         uint8_t *const *d_selected, siting_result *results,
+                         const siting_plan *plans);
 
 /* ---- files (the reference's input and output formats) ------------------ */
 /* Reads exactly nrows*nrows uint16 (siting.cpp:726-730). */

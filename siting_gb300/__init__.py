@@ -21,7 +21,7 @@ import numpy as np
 __all__ = [
     "SitingError", "Params", "Geometry", "Result", "Context", "load", "block_geometry",
     "validate", "fbm_dem", "read_dem", "write_observers", "observers_text", "LIB_PATH",
-    "CLI_PATH", "shed_words",
+    "CLI_PATH", "shed_words", "Plan",
 ]
 
 _PKG = os.path.dirname(os.path.abspath(__file__))
@@ -54,6 +54,23 @@ class _ResultC(C.Structure):
                 ("nwanted", C.c_int), ("ms_vix", C.c_float), ("ms_findmax", C.c_float),
                 ("ms_viewshed", C.c_float), ("ms_site", C.c_float), ("ms_h2d", C.c_float),
                 ("ms_d2h", C.c_float), ("site_rounds", C.c_int)]
+
+
+class _PlanC(C.Structure):
+    _fields_ = [("vix_tile", C.c_int), ("vix_smem", C.c_int), ("shed_smem", C.c_int),
+                ("site_ctas", C.c_int)]
+
+
+@dataclass
+class Plan:
+    """Launch plan of one job; 0 / -1 take the library default."""
+    vix_tile: int = 0
+    vix_smem: int = -1
+    shed_smem: int = -1
+    site_ctas: int = 0
+
+    def c(self) -> _PlanC:
+        return _PlanC(self.vix_tile, self.vix_smem, self.shed_smem, self.site_ctas)
 
 
 @dataclass
@@ -143,6 +160,8 @@ def load() -> C.CDLL:
         "siting_run_dev": ([_P, C.POINTER(_ParamsC), _P, _P, _P, C.POINTER(_ResultC)], i),
         "siting_last_pick_order": ([_P, _P, i, C.POINTER(C.c_int)], i),
         "siting_last_site_phase_cycles": ([_P, _P, i], i),
+        "siting_run_batch": ([_P, i, _P, _P, _P, _P, _P, _P], i),
+        "siting_run_batch_dev": ([_P, i, _P, _P, _P, _P, _P, _P], i),
         "siting_read_dem": ([C.c_char_p, i, _P], i),
         "siting_write_observers": ([C.c_char_p, i, i, _P, _P], i),
         "siting_fbm_dem": ([_P, i, C.c_uint64, i, C.c_double, C.c_double, C.c_double,
@@ -368,3 +387,28 @@ class Context:
         self._check(self._lib.siting_run_dev(self.h, C.byref(pc), _ptr(d_elevs), _ptr(d_obs),
                                              _ptr(d_selected), C.byref(r)))
         return Result.of(r)
+
+    # ---- batched form ---------------------------------------------------------
+    def _batch(self, fn, params, dems, obs, sels, plans):
+        nj = len(params)
+        pa = (_ParamsC * nj)(*[p.c() for p in params])
+        dp = (C.c_void_p * nj)(*[_ptr(d) for d in dems])
+        op = (C.c_void_p * nj)(*[_ptr(o) for o in obs])
+        sp = (C.c_void_p * nj)(*[_ptr(x) for x in sels])
+        res = (_ResultC * nj)()
+        pl = (_PlanC * nj)(*[q.c() for q in plans]) if plans is not None else None
+        self._check(fn(self.h, nj, pa, dp, op, sp, res, pl))
+        return [Result.of(r) for r in res]
+
+    def run_batch(self, params, dems, plans=None):
+        """Host DEMs in; per job (obs, selected, Result)."""
+        dems = [np.ascontiguousarray(d, np.uint16).ravel() for d in dems]
+        geos = [block_geometry(p.nrows, p.bw, p.nwanted0) for p in params]
+        obs = [np.empty(g.nwanted, np.int32) for g in geos]
+        sels = [np.empty(g.nwanted, np.uint8) for g in geos]
+        res = self._batch(self._lib.siting_run_batch, params, dems, obs, sels, plans)
+        return list(zip(obs, sels, res))
+
+    def run_batch_dev(self, params, d_dems, d_obs, d_sels, plans=None):
+        """Device buffers (pointers or tensors) in and out; per job Result."""
+        return self._batch(self._lib.siting_run_batch_dev, params, d_dems, d_obs, d_sels, plans)

@@ -12,40 +12,13 @@
 #include <string>
 #include <vector>
 
+#include "ctx.h"
 #include "kernels.h"
 #include "siting.h"
 
 using namespace siting;
 
-namespace {
-
-struct DevBuf {
-  void *p = nullptr;
-  size_t cap = 0;
-};
-
-enum Slot { kDem, kVix, kObs, kSheds, kTables, kSite, kSel, kErr, kNumSlots };
-
-}  // namespace
-
-struct siting_ctx {
-  int device = 0;
-  int sm_count = 0;
-  cudaStream_t stream = nullptr;
-  size_t budget = 0;
-  size_t held = 0;
-  DevBuf buf[kNumSlots];
-  cudaEvent_t ev[8] = {};
-  std::string err;
-  int site_ctas = 0;  // 0 = automatic
-  int tab_roi = -1, tab_ntests = -1;  // VIX tables currently on the device
-  std::vector<unsigned char> tab_host;
-  long long *h_out = nullptr;  // pinned: SITE outputs + error flag
-  int32_t *d_last_order = nullptr;  // pick order of the last SITE run (in kSite)
-  int last_nused = 0;
-};
-
-namespace {
+namespace siting {
 
 int fail(siting_ctx *ctx, int code, const std::string &msg) {
   if (ctx) ctx->err = msg;
@@ -56,11 +29,35 @@ int cuda_fail(siting_ctx *ctx, cudaError_t e, const char *what) {
   return fail(ctx, SITING_ECUDA, std::string(what) + ": " + cudaGetErrorString(e));
 }
 
-#define CK(call)                                        \
-  do {                                                  \
-    cudaError_t e_ = (call);                            \
-    if (e_ != cudaSuccess) return cuda_fail(ctx, e_, #call); \
-  } while (0)
+int stage_get(siting_ctx *ctx, size_t bytes, unsigned char **out) {
+  if (ctx->h_stage_cap < bytes) {
+    if (ctx->h_stage) {
+      cudaStreamSynchronize(ctx->stream);
+      cudaFreeHost(ctx->h_stage);
+      ctx->h_stage = nullptr;
+      ctx->h_stage_cap = 0;
+    }
+    const size_t want = std::max<size_t>(bytes, 1 << 16);
+    if (cudaMallocHost(reinterpret_cast<void **>(&ctx->h_stage), want) != cudaSuccess) {
+      cudaGetLastError();
+      return fail(ctx, SITING_ENOMEM, "pinned staging allocation failed");
+    }
+    ctx->h_stage_cap = want;
+  }
+  *out = ctx->h_stage;
+  return SITING_OK;
+}
+
+int check_err_flags(siting_ctx *ctx, const int *h, int n) {
+  int f = 0;
+  for (int i = 0; i < n; i++) f |= h[i];
+  if (f & kErrTmaTimeout) return fail(ctx, SITING_ETIMEOUT, "TMA tile wait expired");
+  if (f & kErrBarrierTimeout) return fail(ctx, SITING_ETIMEOUT, "SITE group barrier wait expired");
+  if (f & kErrCapacity) return fail(ctx, SITING_ECUDA, "SITE neighbour list overflow");
+  if (f & kErrSiteMismatch) return fail(ctx, SITING_ECUDA, "SITE self-check failed");
+  if (f & kErrBadInput) return fail(ctx, SITING_EINVAL, "observer index outside the DEM");
+  return SITING_OK;
+}
 
 // Grows workspace slot `s` to at least `bytes` (contents not preserved).
 int ws_get(siting_ctx *ctx, Slot s, size_t bytes, void **out) {
@@ -96,6 +93,41 @@ int ws_get(siting_ctx *ctx, Slot s, size_t bytes, void **out) {
   return SITING_OK;
 }
 
+bool geometry_of(int nrows, int bw, int nwanted0, siting_geometry *g) {
+  // siting.cpp:689-695
+  const float bs = (float)nrows / (int)((float)nrows / bw + 0.5f);
+  const int nb = (int)(nrows / bs + 0.5f);
+  const int npb = (int)((float)nwanted0 / (nb * nb) + 0.99999f);
+  g->blocksize = bs;
+  g->nblocks = nb;
+  g->nwantedperblock = npb;
+  g->nwanted = npb * nb * nb;
+  const int last = nrows - (int)(bs * (nb - 1));
+  return last * last >= npb;
+}
+
+int validate(const siting_params *p, int lib_form, std::string *msg) {
+  // siting.cpp:680-686 (messages kept), then siting.cpp:693-695
+  if (p->nrows <= 0 || p->nrows > 20000) return *msg = "Unreasonable value for nrows", 1;
+  if (p->roi < 1 || p->roi > 10000) return *msg = "Unreasonable value for roi.", 1;
+  if (p->tht < 0 || p->tht > 1000000) return *msg = "Unreasonable value for tht.", 1;
+  if (p->oht < 0 || p->oht > 1000000) return *msg = "Unreasonable value for oht.", 1;
+  if (p->ntests < 1 || p->ntests > 1000) return *msg = "Unreasonable value for ntests.", 1;
+  if (p->bw < (lib_form ? 1 : 10) || p->bw > 2000)
+    return *msg = "Unreasonable value for blocksize0.", 1;
+  if (p->nwanted0 < (lib_form ? 1 : 100) || p->nwanted0 > 2000000)
+    return *msg = "Unreasonable value for nwanted0.", 1;
+  if (p->intervis != 0 && p->intervis != 1) return *msg = "Unreasonable value for intervis.", 1;
+  siting_geometry g;
+  if (!geometry_of(p->nrows, p->bw, p->nwanted0, &g))
+    return *msg = "The last block is too small for nwantedperblock.", 1;
+  return 0;
+}
+
+}  // namespace siting
+
+namespace {
+
 PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
   static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
   static std::once_flag once;
@@ -108,19 +140,6 @@ PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
       fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
   });
   return fn;
-}
-
-bool geometry_of(int nrows, int bw, int nwanted0, siting_geometry *g) {
-  // siting.cpp:689-695
-  const float bs = (float)nrows / (int)((float)nrows / bw + 0.5f);
-  const int nb = (int)(nrows / bs + 0.5f);
-  const int npb = (int)((float)nwanted0 / (nb * nb) + 0.99999f);
-  g->blocksize = bs;
-  g->nblocks = nb;
-  g->nwantedperblock = npb;
-  g->nwanted = npb * nb * nb;
-  const int last = nrows - (int)(bs * (nb - 1));
-  return last * last >= npb;
 }
 
 int check_device(siting_ctx *ctx) {
@@ -164,12 +183,7 @@ int check_err_flag(siting_ctx *ctx, int *d_err) {
   int h = 0;
   CK(cudaMemcpyAsync(&h, d_err, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
   CK(cudaStreamSynchronize(ctx->stream));
-  if (h & kErrTmaTimeout) return fail(ctx, SITING_ETIMEOUT, "TMA tile wait expired");
-  if (h & kErrBarrierTimeout) return fail(ctx, SITING_ETIMEOUT, "SITE group barrier wait expired");
-  if (h & kErrCapacity) return fail(ctx, SITING_ECUDA, "SITE neighbour list overflow");
-  if (h & kErrSiteMismatch) return fail(ctx, SITING_ECUDA, "SITE self-check failed");
-  if (h & kErrBadInput) return fail(ctx, SITING_EINVAL, "observer index outside the DEM");
-  return SITING_OK;
+  return check_err_flags(ctx, &h, 1);
 }
 
 int vix_dev(siting_ctx *ctx, const DemView &dem, int roi, int oht, int tht, int ntests,
@@ -249,24 +263,6 @@ bool obs_in_range(const int32_t *obs, int nsheds, int nrows) {
   for (int i = 0; i < nsheds; i++)
     if (obs[i] < 0 || obs[i] >= ncell) return false;
   return true;
-}
-
-int validate(const siting_params *p, int lib_form, std::string *msg) {
-  // siting.cpp:680-686 (messages kept), then siting.cpp:693-695
-  if (p->nrows <= 0 || p->nrows > 20000) return *msg = "Unreasonable value for nrows", 1;
-  if (p->roi < 1 || p->roi > 10000) return *msg = "Unreasonable value for roi.", 1;
-  if (p->tht < 0 || p->tht > 1000000) return *msg = "Unreasonable value for tht.", 1;
-  if (p->oht < 0 || p->oht > 1000000) return *msg = "Unreasonable value for oht.", 1;
-  if (p->ntests < 1 || p->ntests > 1000) return *msg = "Unreasonable value for ntests.", 1;
-  if (p->bw < (lib_form ? 1 : 10) || p->bw > 2000)
-    return *msg = "Unreasonable value for blocksize0.", 1;
-  if (p->nwanted0 < (lib_form ? 1 : 100) || p->nwanted0 > 2000000)
-    return *msg = "Unreasonable value for nwanted0.", 1;
-  if (p->intervis != 0 && p->intervis != 1) return *msg = "Unreasonable value for intervis.", 1;
-  siting_geometry g;
-  if (!geometry_of(p->nrows, p->bw, p->nwanted0, &g))
-    return *msg = "The last block is too small for nwantedperblock.", 1;
-  return 0;
 }
 
 struct EventTimer {
@@ -378,6 +374,7 @@ int siting_ctx_destroy(siting_ctx *ctx) {
     if (ev) cudaEventDestroy(ev);
   if (ctx->stream) cudaStreamDestroy(ctx->stream);
   if (ctx->h_out) cudaFreeHost(ctx->h_out);
+  if (ctx->h_stage) cudaFreeHost(ctx->h_stage);
   delete ctx;
   return SITING_OK;
 }

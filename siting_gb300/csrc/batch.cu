@@ -1,0 +1,266 @@
+// Batched form: many independent jobs (DEMs of any size and parameters) per
+// call.  VIX, FINDMAX and VIEWSHED of every job are enqueued back to back on
+// the context's stream (each job's grids are large: a tile or an observer per
+// CTA); the greedy SITE selections, whose dependent rounds leave most SMs
+// idle when run one job at a time, run many jobs at once: the jobs' CTA
+// groups are packed into as few cooperative launches as the SM count allows,
+// largest groups first, each group with its own barrier and scratch.  One
+// workspace holds every job's buffers; results are collected after a single
+// synchronisation.
+#include <algorithm>
+#include <numeric>
+#include <vector>
+
+#include "ctx.h"
+#include "kernels.h"
+#include "siting.h"
+
+using namespace siting;
+
+namespace {
+
+struct Job {
+  siting_params p;
+  siting_geometry g;
+  int n, pitch, nr, nwpr, G;
+  size_t per;
+  VixPlan vp;
+  ShedPlan sp;
+  // workspace offsets
+  size_t o_dem, o_vix, o_obs, o_sel, o_sheds, o_tab, o_site, o_err;
+  size_t site_zero;  // bytes of the SITE scratch that start at zero
+};
+
+size_t align256(size_t b) { return (b + 255) & ~(size_t)255; }
+
+// CTAs of a job's SITE group in a batch: the fewest that keep each CTA's
+// candidates within the kernel's per-CTA capacity, so many jobs share the SMs.
+int batch_site_ctas(int nsheds, int sm_count) {
+  const int g = std::max(1, (nsheds + 4095) / 4096);
+  return std::min(std::min(g, std::max(1, nsheds)), sm_count);
+}
+
+int run_batch(siting_ctx *ctx, int njobs, const siting_params *params,
+              const uint16_t *const *elevs, bool host_io, int32_t *const *obs_out,
+              uint8_t *const *sel_out, siting_result *results, const siting_plan *plans) {
+  if (!ctx || njobs < 0 || (njobs && (!params || !elevs || !obs_out || !sel_out)))
+    return fail(ctx, SITING_EINVAL, "run_batch: null argument");
+  if (njobs == 0) return SITING_OK;
+  cudaSetDevice(ctx->device);
+  std::vector<Job> jobs(njobs);
+  size_t ws = 0, tab_bytes = 0;
+  for (int j = 0; j < njobs; j++) {
+    Job &J = jobs[j];
+    J.p = params[j];
+    std::string m;
+    if (validate(&J.p, 1, &m)) return fail(ctx, SITING_EINVAL, "job " + std::to_string(j) + ": " + m);
+    if (!elevs[j] || !obs_out[j] || !sel_out[j])
+      return fail(ctx, SITING_EINVAL, "job " + std::to_string(j) + ": null buffer");
+    geometry_of(J.p.nrows, J.p.bw, J.p.nwanted0, &J.g);
+    J.n = J.p.nrows;
+    J.pitch = (J.n + 7) & ~7;
+    J.nr = 2 * J.p.roi + 1;
+    J.nwpr = (J.nr + 63) / 64;
+    J.per = (size_t)J.nr * J.nwpr;
+    const siting_plan *pl = plans ? &plans[j] : nullptr;
+    J.vp = vix_plan_for(J.n, J.p.roi, J.p.ntests, pl ? pl->vix_tile : 0, pl ? pl->vix_smem : -1);
+    J.sp = shed_plan_for(J.p.roi, pl ? pl->shed_smem : -1);
+    J.G = (pl && pl->site_ctas > 0) ? std::min(pl->site_ctas, ctx->sm_count)
+                                     : batch_site_ctas(J.g.nwanted, ctx->sm_count);
+    if (!site_supported(J.p.roi, J.g.nwanted, J.G))
+      return fail(ctx, SITING_EINVAL, "job " + std::to_string(j) + ": beyond the SITE kernel's limits");
+    if (site_smem_bytes(J.p.roi, J.g.nwanted, J.G, J.g.nblocks, J.g.nwantedperblock,
+                        J.g.blocksize) > 220 * 1024)
+      return fail(ctx, SITING_EINVAL, "job " + std::to_string(j) + ": SITE shared-memory plan too large");
+    J.o_dem = ws;
+    ws += align256((size_t)J.pitch * J.n * 2);
+    J.o_vix = ws;
+    ws += align256((size_t)J.n * J.n);
+    J.o_obs = ws;
+    ws += align256((size_t)J.g.nwanted * 4);
+    J.o_sel = ws;
+    ws += align256((size_t)J.g.nwanted);
+    J.o_sheds = ws;
+    ws += align256((size_t)J.g.nwanted * J.per * 8);
+    J.o_tab = tab_bytes;
+    tab_bytes += align256(vix_table_bytes(J.p.roi, J.p.ntests));
+    J.o_site = ws;
+    ws += align256(site_scratch_bytes(J.n, J.g.nwanted, J.G));
+    J.o_err = ws;
+    ws += 256;
+  }
+  // SITE launches: pack the groups, largest first, into waves of <= sm_count CTAs
+  std::vector<int> order(njobs);
+  std::iota(order.begin(), order.end(), 0);
+  std::stable_sort(order.begin(), order.end(),
+                   [&](int a, int b) { return jobs[a].G > jobs[b].G; });
+  std::vector<std::vector<int>> waves;
+  std::vector<int> wave_ctas;
+  for (int j : order) {
+    size_t w = 0;
+    while (w < waves.size() && wave_ctas[w] + jobs[j].G > ctx->sm_count) w++;
+    if (w == waves.size()) {
+      waves.emplace_back();
+      wave_ctas.push_back(0);
+    }
+    waves[w].push_back(j);
+    wave_ctas[w] += jobs[j].G;
+  }
+  std::vector<size_t> o_wtab(waves.size());
+  size_t wtab_bytes = 0;
+  for (size_t w = 0; w < waves.size(); w++) {
+    o_wtab[w] = wtab_bytes;
+    wtab_bytes += align256(site_job_table_bytes((int)waves[w].size(), wave_ctas[w]));
+  }
+  const size_t o_tabs = ws;
+  ws += align256(tab_bytes);
+  const size_t o_wtabs = ws;
+  ws += align256(wtab_bytes);
+
+  void *base_v;
+  int rc = ws_get(ctx, kBatch, ws, &base_v);
+  if (rc) return rc;
+  unsigned char *base = static_cast<unsigned char *>(base_v);
+  // pinned staging: VIX tables, wave job tables, then per-job readback
+  const size_t s_tabs = 0, s_wtabs = align256(tab_bytes);
+  const size_t s_out = s_wtabs + align256(wtab_bytes);
+  const size_t s_bytes = s_out + (size_t)njobs * 16 * sizeof(long long);
+  unsigned char *stage;
+  if ((rc = stage_get(ctx, s_bytes, &stage))) return rc;
+  cudaStream_t st = ctx->stream;
+
+  CK(cudaEventRecord(ctx->ev[5], st));
+  for (int j = 0; j < njobs; j++) {  // inputs, VIX tables, zeroed scratch
+    Job &J = jobs[j];
+    if (host_io || J.n % 8 || (uintptr_t)elevs[j] % 16)
+      CK(cudaMemcpy2DAsync(base + J.o_dem, (size_t)J.pitch * 2, elevs[j], (size_t)J.n * 2,
+                           (size_t)J.n * 2, J.n,
+                           host_io ? cudaMemcpyHostToDevice : cudaMemcpyDeviceToDevice, st));
+    vix_fill_tables(stage + s_tabs + J.o_tab, J.p.roi, J.p.ntests);
+    SiteScratch s;
+    site_carve_scratch(base + J.o_site, J.n, J.g.nwanted, J.G, &s);
+    J.site_zero = (unsigned char *)s.order - (base + J.o_site);
+    CK(cudaMemsetAsync(base + J.o_site, 0, J.site_zero, st));
+    CK(cudaMemsetAsync(base + J.o_err, 0, 256, st));
+  }
+  CK(cudaMemcpyAsync(base + o_tabs, stage + s_tabs, tab_bytes, cudaMemcpyHostToDevice, st));
+  CK(cudaEventRecord(ctx->ev[0], st));
+  auto dem_of = [&](int j) {
+    const Job &J = jobs[j];
+    const bool own = host_io || J.n % 8 || (uintptr_t)elevs[j] % 16;
+    return own ? DemView{reinterpret_cast<const uint16_t *>(base + J.o_dem), J.n, J.pitch, true}
+               : DemView{elevs[j], J.n, J.n, true};
+  };
+  auto obs_of = [&](int j) {
+    return host_io ? reinterpret_cast<int32_t *>(base + jobs[j].o_obs) : obs_out[j];
+  };
+  auto sel_of = [&](int j) {
+    return host_io ? reinterpret_cast<uint8_t *>(base + jobs[j].o_sel) : sel_out[j];
+  };
+  for (int j = 0; j < njobs; j++) {
+    const Job &J = jobs[j];
+    CK(launch_vix(dem_of(j), J.p.roi, J.p.oht, J.p.tht, J.p.ntests, base + J.o_vix,
+                  base + o_tabs + J.o_tab, J.vp, reinterpret_cast<int *>(base + J.o_err), st));
+  }
+  CK(cudaEventRecord(ctx->ev[1], st));
+  for (int j = 0; j < njobs; j++) {
+    const Job &J = jobs[j];
+    CK(launch_findmax(base + J.o_vix, J.n, J.g.blocksize, J.g.nblocks, J.g.nwantedperblock,
+                      obs_of(j), st));
+  }
+  CK(cudaEventRecord(ctx->ev[2], st));
+  for (int j = 0; j < njobs; j++) {
+    const Job &J = jobs[j];
+    CK(launch_sheds(dem_of(j), J.p.roi, J.p.oht, J.p.tht, J.g.nwanted, obs_of(j),
+                    reinterpret_cast<uint64_t *>(base + J.o_sheds), J.sp,
+                    reinterpret_cast<int *>(base + J.o_err), st));
+  }
+  CK(cudaEventRecord(ctx->ev[3], st));
+  for (size_t w = 0; w < waves.size(); w++) {
+    std::vector<SiteJob> sj;
+    for (int j : waves[w]) {
+      const Job &J = jobs[j];
+      SiteScratch s;
+      site_carve_scratch(base + J.o_site, J.n, J.g.nwanted, J.G, &s);
+      CK(cudaMemsetAsync(sel_of(j), 0, J.g.nwanted, st));
+      sj.push_back(SiteJob{J.n, J.p.roi, J.p.intervis, J.g.nwanted, obs_of(j),
+                           reinterpret_cast<const uint64_t *>(base + J.o_sheds), J.g.blocksize,
+                           J.g.nblocks, J.g.nwantedperblock, sel_of(j), s, J.G,
+                           reinterpret_cast<int *>(base + J.o_err)});
+    }
+    CK(launch_site_jobs(sj.data(), (int)sj.size(), base + o_wtabs + o_wtab[w],
+                        stage + s_wtabs + o_wtab[w], st));
+  }
+  CK(cudaEventRecord(ctx->ev[4], st));
+  // outputs and per-job readback (SITE outputs and error flag)
+  long long *hout = reinterpret_cast<long long *>(stage + s_out);
+  for (int j = 0; j < njobs; j++) {
+    const Job &J = jobs[j];
+    SiteScratch s;
+    site_carve_scratch(base + J.o_site, J.n, J.g.nwanted, J.G, &s);
+    CK(cudaMemcpyAsync(hout + 16 * j, s.out, 3 * sizeof(long long), cudaMemcpyDeviceToHost, st));
+    CK(cudaMemcpyAsync(hout + 16 * j + 8, base + J.o_err, sizeof(int), cudaMemcpyDeviceToHost,
+                       st));
+  }
+  CK(cudaEventRecord(ctx->ev[6], st));
+  if (host_io)
+    for (int j = 0; j < njobs; j++) {
+      const Job &J = jobs[j];
+      CK(cudaMemcpyAsync(obs_out[j], base + J.o_obs, (size_t)J.g.nwanted * 4,
+                         cudaMemcpyDeviceToHost, st));
+      CK(cudaMemcpyAsync(sel_out[j], base + J.o_sel, J.g.nwanted, cudaMemcpyDeviceToHost, st));
+    }
+  CK(cudaEventRecord(ctx->ev[7], st));
+  CK(cudaStreamSynchronize(st));
+  std::vector<int> flags(njobs);
+  for (int j = 0; j < njobs; j++) flags[j] = (int)(hout[16 * j + 8] & 0xffffffff);
+  for (int j = 0; j < njobs; j++)
+    if (flags[j]) {
+      rc = check_err_flags(ctx, &flags[j], 1);
+      ctx->err = "job " + std::to_string(j) + ": " + ctx->err;
+      return rc;
+    }
+  float t[8] = {};
+  cudaEventElapsedTime(&t[0], ctx->ev[5], ctx->ev[0]);
+  cudaEventElapsedTime(&t[1], ctx->ev[0], ctx->ev[1]);
+  cudaEventElapsedTime(&t[2], ctx->ev[1], ctx->ev[2]);
+  cudaEventElapsedTime(&t[3], ctx->ev[2], ctx->ev[3]);
+  cudaEventElapsedTime(&t[4], ctx->ev[3], ctx->ev[4]);
+  cudaEventElapsedTime(&t[5], ctx->ev[6], ctx->ev[7]);
+  if (results)
+    for (int j = 0; j < njobs; j++) {
+      siting_result &r = results[j];
+      r = siting_result{};
+      r.nusedsheds = (int)hout[16 * j];
+      r.cumarea = hout[16 * j + 1];
+      r.coverage = 100.0 * r.cumarea / ((double)jobs[j].n * jobs[j].n);
+      r.nwanted = jobs[j].g.nwanted;
+      r.site_rounds = (int)hout[16 * j + 2];
+      r.ms_h2d = t[0];  // batch-wide phase times
+      r.ms_vix = t[1];
+      r.ms_findmax = t[2];
+      r.ms_viewshed = t[3];
+      r.ms_site = t[4];
+      r.ms_d2h = t[5];
+    }
+  return SITING_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int siting_run_batch(siting_ctx *ctx, int njobs, const siting_params *params,
+                     const uint16_t *const *elevs, int32_t *const *obs, uint8_t *const *selected,
+                     siting_result *results, const siting_plan *plans) {
+  return run_batch(ctx, njobs, params, elevs, true, obs, selected, results, plans);
+}
+
+int siting_run_batch_dev(siting_ctx *ctx, int njobs, const siting_params *params,
+                         const uint16_t *const *d_elevs, int32_t *const *d_obs,
+                         uint8_t *const *d_selected, siting_result *results,
+                         const siting_plan *plans) {
+  return run_batch(ctx, njobs, params, d_elevs, false, d_obs, d_selected, results, plans);
+}
+
+}  // extern "C"

@@ -1,0 +1,60 @@
+// Internal: the siting context and helpers shared by the C ABI's files.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <string>
+#include <vector>
+
+#include "kernels.h"
+#include "siting.h"
+
+namespace siting {
+
+struct DevBuf {
+  void *p = nullptr;
+  size_t cap = 0;
+};
+
+enum Slot { kDem, kVix, kObs, kSheds, kTables, kSite, kSel, kErr, kBatch, kNumSlots };
+
+}  // namespace siting
+
+struct siting_ctx {
+  int device = 0;
+  int sm_count = 0;
+  cudaStream_t stream = nullptr;
+  size_t budget = 0;
+  size_t held = 0;
+  siting::DevBuf buf[siting::kNumSlots];
+  cudaEvent_t ev[8] = {};
+  std::string err;
+  int site_ctas = 0;                  // 0 = automatic
+  int tab_roi = -1, tab_ntests = -1;  // VIX tables currently on the device
+  std::vector<unsigned char> tab_host;
+  long long *h_out = nullptr;         // pinned: SITE outputs
+  int32_t *d_last_order = nullptr;    // pick order of the last SITE run
+  int last_nused = 0;
+  unsigned char *h_stage = nullptr;   // pinned staging for batch uploads/readouts
+  size_t h_stage_cap = 0;
+};
+
+namespace siting {
+
+int fail(siting_ctx *ctx, int code, const std::string &msg);
+int cuda_fail(siting_ctx *ctx, cudaError_t e, const char *what);
+// Grows workspace slot `s` to at least `bytes` (contents not preserved).
+int ws_get(siting_ctx *ctx, Slot s, size_t bytes, void **out);
+// Pinned host staging of at least `bytes`.
+int stage_get(siting_ctx *ctx, size_t bytes, unsigned char **out);
+bool geometry_of(int nrows, int bw, int nwanted0, siting_geometry *g);
+int validate(const siting_params *p, int lib_form, std::string *msg);
+int check_err_flags(siting_ctx *ctx, const int *h_flags, int n);
+
+}  // namespace siting
+
+#define CK(call)                                                        \
+  do {                                                                  \
+    cudaError_t e_ = (call);                                            \
+    if (e_ != cudaSuccess) return siting::cuda_fail(ctx, e_, #call);    \
+  } while (0)

@@ -42,6 +42,8 @@ struct VixPlan {
 size_t vix_table_bytes(int roi, int ntests);
 void vix_fill_tables(void *host_buf, int roi, int ntests);
 VixPlan vix_default_plan(int nrows, int roi, int ntests);
+// A caller's plan (tile 16/32/64, smem 1/0/-1), corrected to one that fits.
+VixPlan vix_plan_for(int nrows, int roi, int ntests, int tile, int smem);
 size_t vix_smem_bytes(const VixPlan &p, int roi, int ntests);
 cudaError_t launch_vix(const DemView &dem, int roi, int oht, int tht, int ntests,
                        uint8_t *vix, const void *d_tables, const VixPlan &plan, int *d_err,
@@ -61,6 +63,7 @@ struct ShedPlan {
   bool use_smem;  // stage the (2roi+1)^2 window by TMA
 };
 ShedPlan shed_default_plan(int roi);
+ShedPlan shed_plan_for(int roi, int smem);
 size_t shed_smem_bytes(const ShedPlan &p, int roi);
 cudaError_t launch_sheds(const DemView &dem, int roi, int oht, int tht, int nsheds,
                          const int32_t *obs, uint64_t *sheds, const ShedPlan &plan, int *d_err,
@@ -77,7 +80,30 @@ struct SiteScratch {
   long long *out;            // [0] nused, [1] cumarea, [2] rounds, [3..9] phase cycles
   int32_t *order;            // nsheds: picks in order
   int32_t *gains;            // nsheds: round-1 gains (site_score_kernel)
+  void *table;               // job table of a one-job launch (site_job_table_bytes)
 };
+
+// One SITE job (one DEM) of a launch.
+struct SiteJob {
+  int nrows, roi, intervis, nsheds;
+  const int32_t *obs;
+  const uint64_t *sheds;
+  float blocksize;
+  int nblocks, npb;
+  uint8_t *selected;
+  SiteScratch scratch;  // zeroed as site_dev does before the launch
+  int nctas;
+  int *err;
+};
+// Device bytes of a job table for `njobs` jobs and `total_ctas` CTAs.
+size_t site_job_table_bytes(int njobs, int total_ctas);
+// Launches the round-1 scoring of every job, then one cooperative launch in
+// which each job's CTAs form their own group.  The sum of nctas must not
+// exceed the number of co-resident CTAs (one per SM).
+// h_stage: page-locked host bytes for the job table (site_job_table_bytes),
+// kept unchanged until the copy has run; NULL stages through pageable memory.
+cudaError_t launch_site_jobs(const SiteJob *jobs, int njobs, void *d_table, void *h_stage,
+                             cudaStream_t st);
 size_t site_scratch_bytes(int nrows, int nsheds, int nctas);
 void site_carve_scratch(void *base, int nrows, int nsheds, int nctas, SiteScratch *s);
 int site_default_ctas(int nsheds, int sm_count);

@@ -31,7 +31,9 @@
 // shed, 128-bit loads) stream all sheds once at HBM bandwidth.
 #include <algorithm>
 #include <cmath>
+#include <cstring>
 #include <mutex>
+#include <vector>
 
 #include "common.cuh"
 #include "kernels.h"
@@ -65,6 +67,7 @@ struct SiteArgs {
   int nslots, pick_items, pick_cap, pair_cap;
   int ncap_words;  // shared-memory words for the round's new bits (0 = none)
   long long stop_area;  // smallest cumarea with 100.0*cumarea/n^2 > 95 (host-computed)
+  int block0;           // first CTA of this job's group in the launch
 };
 
 __device__ __forceinline__ void shed_align(int c0, int &fw, int &fb) {
@@ -131,8 +134,16 @@ __global__ void __launch_bounds__(256) site_score_kernel(const uint64_t *sheds, 
   }
 }
 
-__global__ void __launch_bounds__(kSiteThreads, 1) site_kernel(const SiteArgs a) {
+// One launch runs the greedy selection of one or more jobs (DEMs): CTA b
+// belongs to job block_job[b]; each job's CTAs form their own group with
+// their own barrier, scratch and outputs.
+__global__ void __launch_bounds__(kSiteThreads, 1)
+    site_kernel(const SiteArgs *__restrict__ jobs, const int *__restrict__ block_job) {
   extern __shared__ __align__(16) unsigned char sm[];
+  __shared__ SiteArgs s_args;
+  if (threadIdx.x == 0) s_args = jobs[block_job[blockIdx.x]];
+  __syncthreads();
+  const SiteArgs &a = s_args;
   __shared__ int s_m, s_mcut, s_stop_at, s_done, s_flagv, s_roundcut, s_npair, s_nvalid;
   __shared__ long long s_cum;
   __shared__ int s_poff[kMaxPicks + 1];
@@ -140,7 +151,7 @@ __global__ void __launch_bounds__(kSiteThreads, 1) site_kernel(const SiteArgs a)
   __shared__ int s_rank[kMaxPicks];
   __shared__ unsigned char s_near[kMaxPicks];
 
-  const int G = a.G, k = blockIdx.x;
+  const int G = a.G, k = blockIdx.x - a.block0;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nwarps = blockDim.x >> 5;
   const int n = a.n, roi = a.roi, nr = 2 * roi + 1, nwpr = (nr + 63) / 64;
   const int nch = (nwpr + 1 + 3) / 4;  // 4-word chunks of a placed row (nwpr+1 words)
@@ -836,6 +847,7 @@ size_t scratch_layout(int nrows, int nsheds, int nctas, unsigned char *base, Sit
   unsigned char *ou = take(128);
   unsigned char *od = take((size_t)nsheds * 4);
   unsigned char *gn = take((size_t)nsheds * 4);
+  unsigned char *tb = take(site_job_table_bytes(1, nctas));
   if (s) {
     s->cum[0] = reinterpret_cast<uint64_t *>(c0);
     s->cum[1] = reinterpret_cast<uint64_t *>(c1);
@@ -846,6 +858,7 @@ size_t scratch_layout(int nrows, int nsheds, int nctas, unsigned char *base, Sit
     s->out = reinterpret_cast<long long *>(ou);
     s->order = reinterpret_cast<int32_t *>(od);
     s->gains = reinterpret_cast<int32_t *>(gn);
+    s->table = tb;
   }
   return off;
 }
@@ -908,52 +921,103 @@ bool site_supported(int roi, int nsheds, int nctas) {
   return nslots <= kMaxSlots && nctas <= 160 && roi <= 2000;
 }
 
+namespace {
+
+SiteArgs make_site_args(const SiteJob &j, int block0) {
+  SiteArgs a{};
+  a.n = j.nrows;
+  a.roi = j.roi;
+  a.intervis = j.intervis;
+  a.nsheds = j.nsheds;
+  a.G = j.nctas;
+  a.obs = j.obs;
+  a.sheds = j.sheds;
+  a.bs = j.blocksize;
+  a.nb = j.nblocks;
+  a.npb = j.npb;
+  a.cum0 = j.scratch.cum[0];
+  a.topk = j.scratch.topk;
+  a.cuts = j.scratch.cuts;
+  a.ncount = j.scratch.ncount;
+  a.bar = j.scratch.bar;
+  a.out = j.scratch.out;
+  a.order = j.scratch.order;
+  a.selected = j.selected;
+  a.gains = j.scratch.gains;
+  a.err = j.err;
+  a.nslots = (j.nsheds + j.nctas - 1) / j.nctas;
+  const PickBounds pb = site_pick_bounds(j.roi, j.nsheds, j.nctas, j.nblocks, j.npb, j.blocksize);
+  a.pick_items = pb.items;
+  a.pick_cap = pb.cap;
+  a.pair_cap = site_pair_cap(pb);
+  a.ncap_words =
+      site_ncap_words(site_smem_base(j.roi, j.nsheds, j.nctas, j.nblocks, j.npb, j.blocksize));
+  a.stop_area = site_stop_area(j.nrows);
+  a.block0 = block0;
+  return a;
+}
+
+}  // namespace
+
+size_t site_job_table_bytes(int njobs, int total_ctas) {
+  return (((size_t)njobs * sizeof(SiteArgs) + 255) & ~(size_t)255) + (size_t)total_ctas * 4;
+}
+
+cudaError_t launch_site_jobs(const SiteJob *jobs, int njobs, void *d_table, void *h_stage,
+                             cudaStream_t st) {
+  int total = 0;
+  size_t shm = 0;
+  std::vector<SiteArgs> args(njobs);
+  std::vector<int> block_job;
+  for (int i = 0; i < njobs; i++) {
+    args[i] = make_site_args(jobs[i], total);
+    for (int b = 0; b < jobs[i].nctas; b++) block_job.push_back(i);
+    total += jobs[i].nctas;
+    shm = std::max(shm, site_smem_bytes(jobs[i].roi, jobs[i].nsheds, jobs[i].nctas,
+                                        jobs[i].nblocks, jobs[i].npb, jobs[i].blocksize));
+  }
+  if (total == 0) return cudaSuccess;
+  // job table: arguments, then the CTA -> job map
+  const size_t tbytes = site_job_table_bytes(njobs, total);
+  std::vector<unsigned char> pageable;
+  unsigned char *host = static_cast<unsigned char *>(h_stage);
+  if (!host) {
+    pageable.resize(tbytes);
+    host = pageable.data();
+  }
+  const size_t off = ((size_t)njobs * sizeof(SiteArgs) + 255) & ~(size_t)255;
+  memcpy(host, args.data(), (size_t)njobs * sizeof(SiteArgs));
+  memcpy(host + off, block_job.data(), (size_t)total * 4);
+  cudaError_t e = cudaMemcpyAsync(d_table, host, tbytes, cudaMemcpyHostToDevice, st);
+  if (e != cudaSuccess) return e;
+  int dev = 0, sms = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  for (int i = 0; i < njobs; i++) {  // round-1 gains of every job
+    const SiteJob &j = jobs[i];
+    if (j.nsheds <= 0) continue;
+    const int nr = 2 * j.roi + 1, per = nr * ((nr + 63) / 64);
+    const int sgrid = std::max(1, std::min(sms * 8, (j.nsheds + 7) / 8));
+    site_score_kernel<<<sgrid, 256, 0, st>>>(j.sheds, j.nsheds, per, j.scratch.gains);
+  }
+  e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+  e = cudaFuncSetAttribute(site_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shm);
+  if (e != cudaSuccess) return e;
+  const SiteArgs *d_args = static_cast<const SiteArgs *>(d_table);
+  const int *d_map = reinterpret_cast<const int *>(static_cast<unsigned char *>(d_table) + off);
+  void *kargs[] = {&d_args, &d_map};
+  return cudaLaunchCooperativeKernel((void *)site_kernel, dim3(total), dim3(kSiteThreads), kargs,
+                                     shm, st);
+}
+
 cudaError_t launch_site(int nrows, int roi, int intervis, int nsheds, const int32_t *obs,
                         const uint64_t *sheds, float blocksize, int nblocks, int npb,
                         uint8_t *selected, const SiteScratch &s, int nctas, int *d_err,
                         cudaStream_t st) {
-  SiteArgs a{};
-  a.n = nrows;
-  a.roi = roi;
-  a.intervis = intervis;
-  a.nsheds = nsheds;
-  a.G = nctas;
-  a.obs = obs;
-  a.sheds = sheds;
-  a.bs = blocksize;
-  a.nb = nblocks;
-  a.npb = npb;
-  a.cum0 = s.cum[0];
-  a.topk = s.topk;
-  a.cuts = s.cuts;
-  a.ncount = s.ncount;
-  a.bar = s.bar;
-  a.out = s.out;
-  a.order = s.order;
-  a.selected = selected;
-  a.gains = s.gains;
-  a.err = d_err;
-  a.nslots = (nsheds + nctas - 1) / nctas;
-  const PickBounds pb = site_pick_bounds(roi, nsheds, nctas, nblocks, npb, blocksize);
-  a.pick_items = pb.items;
-  a.pick_cap = pb.cap;
-  a.pair_cap = site_pair_cap(pb);
-  a.ncap_words = site_ncap_words(site_smem_base(roi, nsheds, nctas, nblocks, npb, blocksize));
-  a.stop_area = site_stop_area(nrows);
-  const size_t shm = site_smem_bytes(roi, nsheds, nctas, nblocks, npb, blocksize);
-  const int nr = 2 * roi + 1, per = nr * ((nr + 63) / 64);
-  int dev = 0, sms = 0;
-  cudaGetDevice(&dev);
-  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-  const int sgrid = std::max(1, std::min(sms * 8, (nsheds + 7) / 8));
-  site_score_kernel<<<sgrid, 256, 0, st>>>(sheds, nsheds, per, s.gains);
-  cudaError_t e = cudaGetLastError();
-  if (e != cudaSuccess) return e;
-  e = cudaFuncSetAttribute(site_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shm);
-  if (e != cudaSuccess) return e;
-  void *args[] = {&a};
-  return cudaLaunchCooperativeKernel((void *)site_kernel, dim3(nctas), dim3(kSiteThreads), args,
-                                     shm, st);
+  SiteJob j{nrows, roi, intervis, nsheds, obs, sheds, blocksize, nblocks, npb, selected, s, nctas,
+            d_err};
+  return launch_site_jobs(&j, 1, s.table, nullptr, st);
 }
 
 }  // namespace siting

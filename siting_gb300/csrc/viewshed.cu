@@ -269,6 +269,12 @@ ShedPlan shed_default_plan(int roi) {
   return p;
 }
 
+ShedPlan shed_plan_for(int roi, int smem) {
+  ShedPlan p = shed_default_plan(roi);
+  if (smem == 0) p.use_smem = false;
+  return p;  // the window is staged only where the default allows it
+}
+
 cudaError_t launch_sheds(const DemView &dem, int roi, int oht, int tht, int nsheds,
                          const int32_t *obs, uint64_t *sheds, const ShedPlan &plan, int *d_err,
                          cudaStream_t st) {

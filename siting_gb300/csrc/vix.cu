@@ -265,6 +265,20 @@ VixPlan vix_default_plan(int nrows, int roi, int ntests) {
   return p;
 }
 
+VixPlan vix_plan_for(int nrows, int roi, int ntests, int tile, int smem) {
+  VixPlan p = vix_default_plan(nrows, roi, ntests);
+  if (tile == 16 || tile == 32 || tile == 64) {
+    p.tile = tile;
+    p.use_smem = smem != 0;
+    const HaloGeom g = halo_geom(tile, roi);
+    if (p.use_smem && (g.w > 256 || vix_smem_bytes(p, roi, ntests) > 220 * 1024)) p.use_smem = false;
+    if (!p.use_smem && vix_smem_bytes(p, roi, ntests) > 220 * 1024) p = vix_default_plan(nrows, roi, ntests);
+  } else if (smem == 0) {
+    p.use_smem = false;
+  }
+  return p;
+}
+
 cudaError_t launch_vix(const DemView &dem, int roi, int oht, int tht, int ntests, uint8_t *vix,
                        const void *d_tables, const VixPlan &plan, int *d_err, cudaStream_t st) {
   VixArgs a{};

@@ -1,0 +1,78 @@
+"""Batched form: every job of a mixed batch equals the oracle (and so the
+plain single-job path) bit for bit, whatever the launch plan."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def _mixed_jobs(native, n_jobs, seed, sizes=(96, 400), rois=(8, 60)):
+    """A mix in the shape of the batched workload: log-uniform sides (multiples
+    of 8 and not), per-job amplitude, roi, height, targets, bw, nwanted =
+    cells/64 and alternating intervis."""
+    rng = np.random.default_rng(seed)
+    jobs = []
+    for j in range(n_jobs):
+        n = int(np.exp(rng.uniform(np.log(sizes[0]), np.log(sizes[1]))))
+        if j % 3 == 0:
+            n = (n + 31) // 32 * 32
+        p = native.Params(nrows=n, roi=int(rng.integers(*rois)), height=int(rng.integers(5, 60)),
+                          ntests=int(rng.choice([16, 32, 64])), bw=int(rng.choice([8, 16, 32])),
+                          nwanted0=max(1, n * n // 64), intervis=j % 2)
+        dem = native.fbm_dem(n, 900 + seed * 100 + j, octaves=7,
+                             range_max=int(rng.integers(2000, 30000)))
+        jobs.append((p, dem))
+    return jobs
+
+
+def _check_job(oracle, p, dem, obs, sel, res):
+    want = oracle.run(dem, p.nrows, p.roi, p.height, p.ntests, p.bw, p.nwanted0, p.intervis)
+    assert np.array_equal(obs, want["obs"]), "observers differ"
+    assert np.array_equal(sel, want["selected"]), \
+        f"selection differs in {int(np.count_nonzero(sel != want['selected']))} entries"
+    assert (res.nusedsheds, res.cumarea) == (want["nused"], want["cumarea"])
+
+
+def test_batch_matches_oracle(ctx, oracle, native):
+    jobs = _mixed_jobs(native, 10, 1)
+    out = ctx.run_batch([p for p, _ in jobs], [d for _, d in jobs])
+    for (p, dem), (obs, sel, res) in zip(jobs, out):
+        _check_job(oracle, p, dem, obs, sel, res)
+
+
+@pytest.mark.parametrize("plan", [
+    dict(vix_tile=16, vix_smem=1, shed_smem=1, site_ctas=1),
+    dict(vix_tile=64, vix_smem=0, shed_smem=0, site_ctas=3),
+    dict(vix_tile=32, vix_smem=1, shed_smem=-1, site_ctas=16),
+])
+def test_batch_plans_do_not_change_results(ctx, oracle, native, plan):
+    jobs = _mixed_jobs(native, 5, 2)
+    plans = [native.Plan(**plan)] * len(jobs)
+    out = ctx.run_batch([p for p, _ in jobs], [d for _, d in jobs], plans)
+    for (p, dem), (obs, sel, res) in zip(jobs, out):
+        _check_job(oracle, p, dem, obs, sel, res)
+
+
+def test_batch_dev_matches_host(ctx, native):
+    torch = pytest.importorskip("torch")
+    jobs = _mixed_jobs(native, 6, 3)
+    host = ctx.run_batch([p for p, _ in jobs], [d for _, d in jobs])
+    d_dems = [torch.from_numpy(d.view(np.int16)).cuda() for _, d in jobs]
+    geos = [native.block_geometry(p.nrows, p.bw, p.nwanted0) for p, _ in jobs]
+    d_obs = [torch.empty(g.nwanted, dtype=torch.int32, device="cuda") for g in geos]
+    d_sel = [torch.empty(g.nwanted, dtype=torch.uint8, device="cuda") for g in geos]
+    torch.cuda.synchronize()
+    res = ctx.run_batch_dev([p for p, _ in jobs], d_dems, d_obs, d_sel)
+    for (obs, sel, r0), o, s, r1 in zip(host, d_obs, d_sel, res):
+        assert np.array_equal(o.cpu().numpy(), obs)
+        assert np.array_equal(s.cpu().numpy(), sel)
+        assert (r0.nusedsheds, r0.cumarea) == (r1.nusedsheds, r1.cumarea)
+
+
+def test_batch_equals_single_job_runs(ctx, native):
+    jobs = _mixed_jobs(native, 4, 4, sizes=(200, 520), rois=(20, 90))
+    out = ctx.run_batch([p for p, _ in jobs], [d for _, d in jobs])
+    for (p, dem), (obs, sel, res) in zip(jobs, out):
+        o2, s2, r2 = ctx.run(p, dem)
+        assert np.array_equal(obs, o2) and np.array_equal(sel, s2)
+        assert (res.nusedsheds, res.cumarea) == (r2.nusedsheds, r2.cumarea)
