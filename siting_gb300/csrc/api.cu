@@ -278,14 +278,20 @@ struct EventTimer {
 
 namespace siting {
 
+// The DEM is described to TMA as a 3-D tensor {8, pitch/8, rows}: rows of
+// 8-element (16-byte) groups.  A box {8, box_w/8, box_h} then lands in shared
+// memory as a dense box_h x box_w row-major window of up to 2048 columns (a
+// 2-D box is limited to 256 columns), and the innermost coordinate is always
+// 0, so every copy starts on a 16-byte boundary.  box_w must be a multiple of
+// 8 and window origins columns multiples of 8.
 bool make_dem_tensor_map(CUtensorMap *map, const DemView &dem, int box_w, int box_h) {
   PFN_cuTensorMapEncodeTiled_v12000 fn = encode_fn();
-  if (!fn || !dem.tma_ok) return false;
-  cuuint64_t dims[2] = {(cuuint64_t)dem.nrows, (cuuint64_t)dem.nrows};
-  cuuint64_t strides[1] = {(cuuint64_t)dem.pitch * 2};
-  cuuint32_t box[2] = {(cuuint32_t)box_w, (cuuint32_t)box_h};
-  cuuint32_t estr[2] = {1, 1};
-  CUresult r = fn(map, CU_TENSOR_MAP_DATA_TYPE_UINT16, 2, const_cast<uint16_t *>(dem.data), dims,
+  if (!fn || !dem.tma_ok || box_w % 8 || box_w > 2048 || box_h > 256 || dem.pitch % 8) return false;
+  cuuint64_t dims[3] = {8, (cuuint64_t)dem.pitch / 8, (cuuint64_t)dem.nrows};
+  cuuint64_t strides[2] = {16, (cuuint64_t)dem.pitch * 2};
+  cuuint32_t box[3] = {8, (cuuint32_t)box_w / 8, (cuuint32_t)box_h};
+  cuuint32_t estr[3] = {1, 1, 1};
+  CUresult r = fn(map, CU_TENSOR_MAP_DATA_TYPE_UINT16, 3, const_cast<uint16_t *>(dem.data), dims,
                   strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
                   CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
   return r == CUDA_SUCCESS;

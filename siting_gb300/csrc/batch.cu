@@ -23,6 +23,7 @@ struct Job {
   siting_params p;
   siting_geometry g;
   int n, pitch, nr, nwpr, G;
+  bool auto_G;  // SITE group size chosen here (not by the caller's plan)
   size_t per;
   VixPlan vp;
   ShedPlan sp;
@@ -38,6 +39,11 @@ size_t align256(size_t b) { return (b + 255) & ~(size_t)255; }
 int batch_site_ctas(int nsheds, int sm_count) {
   const int g = std::max(1, (nsheds + 4095) / 4096);
   return std::min(std::min(g, std::max(1, nsheds)), sm_count);
+}
+
+bool site_fits(const Job &J, int G) {
+  return site_smem_bytes(J.p.roi, J.g.nwanted, G, J.g.nblocks, J.g.nwantedperblock,
+                         J.g.blocksize) <= 220 * 1024;
 }
 
 int run_batch(siting_ctx *ctx, int njobs, const siting_params *params,
@@ -69,25 +75,9 @@ int run_batch(siting_ctx *ctx, int njobs, const siting_params *params,
                                      : batch_site_ctas(J.g.nwanted, ctx->sm_count);
     if (!site_supported(J.p.roi, J.g.nwanted, J.G))
       return fail(ctx, SITING_EINVAL, "job " + std::to_string(j) + ": beyond the SITE kernel's limits");
-    if (site_smem_bytes(J.p.roi, J.g.nwanted, J.G, J.g.nblocks, J.g.nwantedperblock,
-                        J.g.blocksize) > 220 * 1024)
+    J.auto_G = !(pl && pl->site_ctas > 0);
+    if (!site_fits(J, J.G))
       return fail(ctx, SITING_EINVAL, "job " + std::to_string(j) + ": SITE shared-memory plan too large");
-    J.o_dem = ws;
-    ws += align256((size_t)J.pitch * J.n * 2);
-    J.o_vix = ws;
-    ws += align256((size_t)J.n * J.n);
-    J.o_obs = ws;
-    ws += align256((size_t)J.g.nwanted * 4);
-    J.o_sel = ws;
-    ws += align256((size_t)J.g.nwanted);
-    J.o_sheds = ws;
-    ws += align256((size_t)J.g.nwanted * J.per * 8);
-    J.o_tab = tab_bytes;
-    tab_bytes += align256(vix_table_bytes(J.p.roi, J.p.ntests));
-    J.o_site = ws;
-    ws += align256(site_scratch_bytes(J.n, J.g.nwanted, J.G));
-    J.o_err = ws;
-    ws += 256;
   }
   // SITE launches: pack the groups, largest first, into waves of <= sm_count CTAs
   std::vector<int> order(njobs);
@@ -105,6 +95,45 @@ int run_batch(siting_ctx *ctx, int njobs, const siting_params *params,
     }
     waves[w].push_back(j);
     wave_ctas[w] += jobs[j].G;
+  }
+  // a wave lasts as long as its slowest group: SMs a wave leaves free go to
+  // its automatically planned groups in proportion to their candidates (a
+  // group's rounds shorten with more CTAs), up to the single-job default
+  for (size_t w = 0; w < waves.size(); w++) {
+    const int spare = ctx->sm_count - wave_ctas[w];
+    double total = 0;
+    for (int j : waves[w])
+      if (jobs[j].auto_G) total += jobs[j].g.nwanted;
+    if (spare <= 0 || total <= 0) continue;
+    for (int j : waves[w]) {
+      Job &J = jobs[j];
+      if (!J.auto_G) continue;
+      const int cap = site_default_ctas(J.g.nwanted, ctx->sm_count);
+      const int want = std::min(cap, J.G + (int)(spare * (J.g.nwanted / total)));
+      if (want > J.G && site_supported(J.p.roi, J.g.nwanted, want) && site_fits(J, want)) {
+        wave_ctas[w] += want - J.G;
+        J.G = want;
+      }
+    }
+  }
+  for (int j = 0; j < njobs; j++) {
+    Job &J = jobs[j];
+    J.o_dem = ws;
+    ws += align256((size_t)J.pitch * J.n * 2);
+    J.o_vix = ws;
+    ws += align256((size_t)J.n * J.n);
+    J.o_obs = ws;
+    ws += align256((size_t)J.g.nwanted * 4);
+    J.o_sel = ws;
+    ws += align256((size_t)J.g.nwanted);
+    J.o_sheds = ws;
+    ws += align256((size_t)J.g.nwanted * J.per * 8);
+    J.o_tab = tab_bytes;
+    tab_bytes += align256(vix_table_bytes(J.p.roi, J.p.ntests));
+    J.o_site = ws;
+    ws += align256(site_scratch_bytes(J.n, J.g.nwanted, J.G));
+    J.o_err = ws;
+    ws += 256;
   }
   std::vector<size_t> o_wtab(waves.size());
   size_t wtab_bytes = 0;

@@ -26,8 +26,14 @@ __device__ __forceinline__ float fadd(float a, float b) { return __fadd_rn(a, b)
 __device__ __forceinline__ float fdiv(float a, float b) { return __fdiv_rn(a, b); }
 __device__ __forceinline__ float i2f(int v) { return __int2float_rn(v); }
 __device__ __forceinline__ int f2i(float v) { return __float2int_rz(v); }
-// (int)round(v): half away from zero, as C's round()/roundf().
-__device__ __forceinline__ int round_i(float v) { return __float2int_rz(roundf(v)); }
+// (int)roundf(v), half away from zero, for |v| < 2^31: truncation of
+// v + copysign(pred(0.5), v), with pred(0.5) = 0.5 - 2^-25 the float just
+// below one half (the usual trunc-based round: adding 0.5 itself would round
+// 0.5 - 2^-25 up to 1).  Checked against roundf over every float in range.
+__device__ __forceinline__ int round_i(float v) {
+  const float h = __uint_as_float((__float_as_uint(v) & 0x80000000u) | 0x3effffffu);
+  return __float2int_rz(__fadd_rn(v, h));
+}
 
 // ---- memory-order helpers --------------------------------------------------
 __device__ __forceinline__ unsigned ld_acquire_u32(const unsigned *p) {
@@ -75,13 +81,15 @@ __device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity) {
   }
 }
 
-// 2-D tiled TMA load of box {c0 (inner, elements), r0 (outer)} into smem.
-__device__ __forceinline__ void tma_load_2d(void *dst, const CUtensorMap *map, int c0, int r0,
-                                            uint64_t *bar) {
+// TMA load of a DEM window (3-D map of make_dem_tensor_map): columns from
+// y0 (a multiple of 8) and rows from x0, into dense row-major shared memory.
+// Out-of-DEM rows and columns are filled with zeros.
+__device__ __forceinline__ void tma_load_window(void *dst, const CUtensorMap *map, int y0, int x0,
+                                                uint64_t *bar) {
   asm volatile(
-      "cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes"
-      " [%0], [%1, {%2, %3}], [%4];" ::"r"(smem_u32(dst)),
-      "l"(reinterpret_cast<uint64_t>(map)), "r"(c0), "r"(r0), "r"(smem_u32(bar))
+      "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes"
+      " [%0], [%1, {%2, %3, %4}], [%5];" ::"r"(smem_u32(dst)),
+      "l"(reinterpret_cast<uint64_t>(map)), "r"(0), "r"(y0 >> 3), "r"(x0), "r"(smem_u32(bar))
       : "memory");
 }
 

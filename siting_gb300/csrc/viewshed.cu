@@ -15,7 +15,7 @@
 // step and have nearly equal ray lengths).  Visible cells are OR-ed into a
 // shared-memory image of the shed (32-bit halves of the reference's 64-bit
 // words), which is then written to HBM with coalesced stores.  For windows
-// wider than one TMA box the DEM is read through the read-only L1 path.
+// too large for two CTAs per SM the DEM is read through the read-only L1 path.
 //
 // Bit-exactness: separately rounded FP32 operations, IEEE division for the
 // slopes, round-half-away-from-zero for the minor coordinate.
@@ -66,21 +66,19 @@ struct GlobalDem {
 // The shed is assembled in two shared-memory bit images.  Rays that step
 // along y put a warp's lanes on different rows at each step; they mark cells in
 // the row-major image R (word = row*rs + col/32, bit 31 - col%32, i.e. the
-// reference's MSB-first order split into 32-bit halves).  Rays that step along
-// x put the lanes on one row; they mark the column-major image C (word =
-// col*cs + row/32, bit row%32), where their words differ.  rs and cs are odd,
-// so distinct words also fall in distinct banks.  C is transposed into R at
-// the end, 32x32 bits per warp with ballots.
+// reference's words split into 32-bit halves, bit col%32 LSB-first; the
+// halves are bit-reversed into the reference's MSB-first order on the way
+// out).  Rays that step along x put the lanes on one row; they mark the
+// column-major image C (word = col*cs + row/32, bit row%32), where their words
+// differ.  rs and cs are odd, so distinct words also fall in distinct banks.
+// C is transposed into R at the end, 32x32 bits per warp.
 struct ShedImage {
   unsigned *R, *C;
   int rs, cs;
 };
 
 __device__ __forceinline__ void mark_row_major(const ShedImage &im, int row, int col) {
-  atomicOr(&im.R[row * im.rs + (col >> 5)], 1u << (31 - (col & 31)));
-}
-__device__ __forceinline__ void mark_col_major(const ShedImage &im, int row, int col) {
-  atomicOr(&im.C[col * im.cs + (row >> 5)], 1u << (row & 31));
+  atomicOr(&im.R[row * im.rs + (col >> 5)], 1u << (col & 31));
 }
 
 template <class Dem>
@@ -92,7 +90,7 @@ __device__ __forceinline__ void sweep_rays(const Dem &dem, const ShedArgs &a, in
   const int W = dem.stride();
   const int obase = dem.base(ox, oy);
   const int oalt = dem.at(obase) + a.oht;
-  const float foalt = i2f(oalt);
+  const float foalt = i2f(oalt), ftht = i2f(a.tht);
   for (int ip = threadIdx.x; ip < 4 * side; ip += blockDim.x) {
     int tx, ty;
     if (ip < side) {
@@ -114,34 +112,49 @@ __device__ __forceinline__ void sweep_rays(const Dem &dem, const ShedArgs &a, in
     const int dmaj = my ? dy : dx, dmin = my ? dx : dy;
     const float slope = fdiv(i2f(dmin), i2f(dmaj));
     const int dir = dmaj > 0 ? 1 : -1;
-    // The ray leaves the DEM along the major axis after kedge steps and along
-    // the minor axis when the minor offset leaves [offlo, offhi]; both end it,
-    // as does leaving the roi circle (siting.cpp:333-334).
+    // i*slope = |i| * (dir*slope) exactly (negation is exact), so the minor
+    // offset of step k is round(k * sl).
+    const float sl = dir > 0 ? slope : -slope;
     const int omaj = my ? oy : ox, omin = my ? ox : oy;
-    const int kedge = dir > 0 ? n - 1 - omaj : omaj;
-    const int kend = min(dmaj * dir, kedge);
+    // The ray stops at the DEM edge along the major axis (kedge steps), when
+    // the minor coordinate leaves the DEM, or outside the roi circle
+    // (siting.cpp:333-334).  |round(k*sl)| never decreases with k, so the last
+    // two hold from some step on and a binary search finds the last step.
+    int lo = 0, hi = min(dmaj * dir, dir > 0 ? n - 1 - omaj : omaj);
+    while (lo < hi) {
+      const int mid = (lo + hi + 1) >> 1;
+      const int off = round_i(fmul(i2f(mid), sl));
+      if ((unsigned)(omin + off) < (unsigned)n && mid * mid + off * off <= roi2)
+        lo = mid;
+      else
+        hi = mid - 1;
+    }
+    const int kend = lo;
     const int smaj = my ? dir : dir * W, smin = my ? W : 1;
-    float hs = -99999.f, fai = 0.f;
-    for (int k = 1; k <= kend; k++) {
-      fai = fadd(fai, 1.f);  // (float)|i|, exact
-      const int off = round_i(fmul(dir > 0 ? fai : -fai, slope));  // round(i * slope)
-      if ((unsigned)(omin + off) >= (unsigned)n) break;
-      if (k * k + off * off > roi2) break;
-      const int pelev = dem.at(obase + k * smaj + off * smin);
-      const float fa = i2f(pelev - oalt);
+    // y-major rays mark the row-major image (line = row), x-major rays the
+    // column-major one (line = column); pos is the cell's coordinate along
+    // the ray's axis, bit pos%32 of word line*stride + pos/32
+    unsigned *img = my ? im.R : im.C;
+    const int stride = my ? im.rs : im.cs;
+    int pb = obase, pos = roi;
+    const float fend = i2f(kend);
+    // elevations and offsets are integers below 2^24: their differences and
+    // sums are exact in FP32, so (float)(pelev - oalt) = pelev_f - foalt
+    float hs = -99999.f;
+    for (float fai = 1.f; fai <= fend; fai = fadd(fai, 1.f)) {  // fai = (float)|i|, exact
+      pb += smaj;
+      pos += dir;
+      const int off = round_i(fmul(fai, sl));
+      const float fe = i2f(dem.at(pb + off * smin));
+      const float fa = __fsub_rn(fe, foalt);
       // s = RN(a/|i|) can exceed hs only if a > hs*|i|; the sign of the fused
       // hs*|i| - a is exact, so the division runs only when the horizon may rise
       if (__fmaf_rn(hs, fai, -fa) < 0.f) {
         const float s = fdiv(fa, fai);
         if (hs < s) hs = s;
       }
-      if (i2f(pelev + a.tht) >= fadd(foalt, fmul(hs, fai))) {
-        const int i = dir * k;
-        if (my)
-          mark_row_major(im, off + roi, i + roi);
-        else
-          mark_col_major(im, i + roi, off + roi);
-      }
+      if (fadd(fe, ftht) >= fadd(foalt, fmul(hs, fai)))
+        atomicOr(&img[(off + roi) * stride + (pos >> 5)], 1u << (pos & 31));
     }
   }
 }
@@ -176,7 +189,8 @@ __device__ __forceinline__ void shed_body(const CUtensorMap &map, const ShedArgs
     mbar_init(mbar, 1);
     mbar_expect_tx(mbar, win_bytes);
     for (int b = 0; b < a.nboxes; b++)
-      tma_load_2d(win + (size_t)b * a.box_rows * a.win_w, &map, hy0, hx0 + b * a.box_rows, mbar);
+      tma_load_window(win + (size_t)b * a.box_rows * a.win_w, &map, hy0, hx0 + b * a.box_rows,
+                      mbar);
   }
   for (int i = threadIdx.x; i < img_words; i += blockDim.x) im.R[i] = 0u;
   __syncthreads();
@@ -193,7 +207,7 @@ __device__ __forceinline__ void shed_body(const CUtensorMap &map, const ShedArgs
   __syncthreads();
   // fold C into R: one warp per 32x32 block; lane j holds column cb*32+j's
   // bits of rows rb*32..+31, a 5-stage butterfly transpose leaves row rb*32+i
-  // in lane i (bit j = column cb*32+j), reversed into R's MSB-first order
+  // in lane i (bit j = column cb*32+j), R's own bit order
   const int nb32 = (nr + 31) / 32;
   const int lane = threadIdx.x & 31;
   for (int blk = threadIdx.x >> 5; blk < nb32 * nb32; blk += blockDim.x >> 5) {
@@ -208,13 +222,13 @@ __device__ __forceinline__ void shed_body(const CUtensorMap &map, const ShedArgs
       x = (lane & sh) ? (x & ~m) | ((o >> sh) & m) : (x & m) | ((o << sh) & ~m);
     }
     const int row = rb * 32 + lane;
-    if (row < nr && x) im.R[row * im.rs + cb] |= __brev(x);
+    if (row < nr && x) im.R[row * im.rs + cb] |= x;
   }
   __syncthreads();
   uint64_t *dst = a.sheds + (size_t)blockIdx.x * nwords;
   for (int i = threadIdx.x; i < nwords; i += blockDim.x) {
     const int r = i / nwpr, q = i - r * nwpr;
-    const unsigned hi = im.R[r * im.rs + 2 * q], lo = im.R[r * im.rs + 2 * q + 1];
+    const unsigned hi = __brev(im.R[r * im.rs + 2 * q]), lo = __brev(im.R[r * im.rs + 2 * q + 1]);
     dst[i] = ((uint64_t)hi << 32) | lo;
   }
 }
@@ -264,8 +278,10 @@ ShedPlan shed_default_plan(int roi) {
   const int rounds = (rays + 1023) / 1024;
   const int threads = std::min(1024, ((rays + rounds - 1) / rounds + 31) / 32 * 32);
   ShedPlan p{std::max(threads, 64), true};
-  const WinGeom g = win_geom(roi);
-  if (g.w > 256 || shed_smem_bytes(p, roi) > 110 * 1024) p.use_smem = false;
+  // the window is staged only while two CTAs still share an SM: a ray's steps
+  // form one dependent chain, so a single CTA per SM cannot hide the
+  // shared-memory latency and the L1 path with more resident CTAs is faster
+  if (shed_smem_bytes(p, roi) > 112 * 1024) p.use_smem = false;
   return p;
 }
 

@@ -6,14 +6,14 @@
 // 255.999f)).
 //
 // GB300 mapping: one CTA per T x T cell tile.  The tile's halo (T+2roi rows,
-// T+2roi+7 columns rounded to 8) is loaded into shared memory by one TMA
-// bulk-tensor copy, so every line-of-sight sample is a shared-memory gather.
+// T+2roi+7 columns rounded to 8) is loaded into shared memory by TMA
+// bulk-tensor copies, so every line-of-sight sample is a shared-memory gather.
 // Warps split the tile's cells evenly and walk the flat (cell, target) space
 // 32 items at a time; the target of item (cell, t) comes from the LCG state
 // after 2t+1 steps from the seed, obtained by an affine jump-ahead table
 // instead of a serial chain.  Per-cell hit counts accumulate in shared memory
 // and become VIX bytes through a host-computed table.  When the halo does not
-// fit a single TMA box (large roi) the same code reads the DEM through the
+// fit in shared memory (large roi) the same code reads the DEM through the
 // read-only L1 path instead.
 //
 // Bit-exactness: every FP32 operation is separately rounded (no FMA), the
@@ -170,8 +170,8 @@ __global__ void __launch_bounds__(1024) vix_kernel(const __grid_constant__ CUten
     mbar_init(mbar, 1);
     mbar_expect_tx(mbar, halo_bytes);
     for (int b = 0; b < a.nboxes; b++)
-      tma_load_2d(halo + (size_t)b * a.box_rows * a.halo_w, &map, hy0, hx0 + b * a.box_rows,
-                  mbar);
+      tma_load_window(halo + (size_t)b * a.box_rows * a.halo_w, &map, hy0, hx0 + b * a.box_rows,
+                      mbar);
   }
   for (int i = threadIdx.x; i < a.ntests; i += blockDim.x)
     jump[i] = make_uint2(a.jump[2 * i], a.jump[2 * i + 1]);
@@ -252,16 +252,22 @@ size_t vix_smem_bytes(const VixPlan &p, int roi, int ntests) {
   return b;
 }
 
+// Two 1024-thread CTAs share an SM when each takes at most half of its 228 KB
+// shared memory (31 registers a thread); the second CTA fills the issue slots
+// that the first leaves while its warps drain at the end of a tile.
+constexpr size_t kVixTwoCtaSmem = 112 * 1024;
+constexpr size_t kVixMaxSmem = 220 * 1024;
+
 VixPlan vix_default_plan(int nrows, int roi, int ntests) {
   (void)nrows;
-  VixPlan p{32, 1024, false};
-  const size_t limit = 220 * 1024;
+  // the largest tile whose halo fits two CTAs per SM; else the L1 path, where
+  // a larger halo costs nothing
   for (int tile : {64, 32, 16}) {
     VixPlan q{tile, 1024, true};
-    const HaloGeom g = halo_geom(tile, roi);
-    if (g.w <= 256 && vix_smem_bytes(q, roi, ntests) <= limit) return q;
+    if (vix_smem_bytes(q, roi, ntests) <= kVixTwoCtaSmem) return q;
   }
-  if (vix_smem_bytes(p, roi, ntests) > limit) p.tile = 16;
+  VixPlan p{32, 1024, false};
+  if (vix_smem_bytes(p, roi, ntests) > kVixMaxSmem) p.tile = 16;
   return p;
 }
 
@@ -271,8 +277,8 @@ VixPlan vix_plan_for(int nrows, int roi, int ntests, int tile, int smem) {
     p.tile = tile;
     p.use_smem = smem != 0;
     const HaloGeom g = halo_geom(tile, roi);
-    if (p.use_smem && (g.w > 256 || vix_smem_bytes(p, roi, ntests) > 220 * 1024)) p.use_smem = false;
-    if (!p.use_smem && vix_smem_bytes(p, roi, ntests) > 220 * 1024) p = vix_default_plan(nrows, roi, ntests);
+    if (p.use_smem && (g.w > 2048 || vix_smem_bytes(p, roi, ntests) > kVixMaxSmem)) p.use_smem = false;
+    if (!p.use_smem && vix_smem_bytes(p, roi, ntests) > kVixMaxSmem) p = vix_default_plan(nrows, roi, ntests);
   } else if (smem == 0) {
     p.use_smem = false;
   }

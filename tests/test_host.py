@@ -121,3 +121,21 @@ def test_cli_argument_errors(native, tmp_path):
     assert (r.returncode, r.stdout) == (1, "ERROR: Unreasonable value for blocksize0.\n")
     r = _cli([100, 50, 100, 50, 10, 10000, 0, "missing.bin", "out"], tmp_path)
     assert (r.returncode, r.stdout.splitlines()[-1]) == (1, "ERROR: Input failed")
+
+
+def test_trunc_based_round_matches_roundf():
+    """The kernels' (int)roundf(v) is trunc(v + copysign(0.5 - 2^-25, v)) in
+    FP32.  Checked here against exact half-away-from-zero rounding (in
+    float64) on every float near a half-integer below 2^12 and on a random
+    sample of all floats below 2^31."""
+    rng = np.random.default_rng(7)
+    halves = (np.arange(-4096, 4096, dtype=np.float64) + 0.5).astype(np.float32)
+    near = halves.view(np.int32)[:, None] + np.arange(-64, 65, dtype=np.int32)[None, :]
+    bits = rng.integers(0, 2**32, size=4_000_000, dtype=np.uint64).astype(np.uint32)
+    v = np.concatenate([near.ravel().view(np.float32), bits.view(np.float32)])
+    v = v[np.isfinite(v) & (np.abs(v) < 2.0**31 - 128)]
+    h = np.where(np.signbit(v), np.float32(-0.49999997), np.float32(0.49999997)).astype(np.float32)
+    got = np.trunc(v + h).astype(np.int64)  # float32 + float32: one IEEE rounding
+    x = v.astype(np.float64)
+    want = (np.sign(x) * np.floor(np.abs(x) + 0.5)).astype(np.int64)
+    assert np.array_equal(got, want)
