@@ -279,6 +279,17 @@ def stage_bytes(w, nwanted):
     }
 
 
+# DRAM traffic per unit (dram__bytes_read.sum + dram__bytes_write.sum) from
+# one ncu capture of the 2048^2 case with the 4096^2 workload's parameters
+# (profiles/vix_kernel_c2_2048.md, profiles/shed_kernel2_c2_2048.md), scaled
+# to a launch by the units it processes; VIX traffic grows with the cells,
+# VIEWSHED's with the observers.
+NCU_TRAFFIC_PER_UNIT = {
+    "c2_4096": {"vix": ("cells", 8.406016e6 / 2048 ** 2),
+                "viewshed": ("observers", (8.475392e6 + 55.5584e6) / 16384)},
+}
+
+
 def roofline(out, w, state, peaks, stage_ms_mean):
     """Roofline of the dominant stage (largest mean device time)."""
     dem, d_obs, d_sel, r, ctx, g = state
@@ -294,13 +305,19 @@ def roofline(out, w, state, peaks, stage_ms_mean):
     obs = d_obs.cpu().numpy()
     order = ctx.last_pick_order(g.nwanted)
     site_ref_bytes = site_algorithmic_bytes(w["nrows"], w["roi"], obs, order, g.nwanted)
+    traffic = None
+    per_unit = NCU_TRAFFIC_PER_UNIT.get(out["config"]["workload"], {}).get(dom)
+    if per_unit:
+        units = w["nrows"] ** 2 if per_unit[0] == "cells" else g.nwanted
+        traffic = per_unit[1] * units
     line = {"kernel": dom, "bound": "hbm", "achieved": d["achieved_gbs"], "peak": hbm,
-            "unit": "GB/s", "frac": d["frac"], "traffic": None,
+            "unit": "GB/s", "frac": d["frac"], "traffic": traffic,
             "peak_source": f"{src} (MEASURED_PEAKS.json hbm_gbs)" if src == "measured" else
             "fallback 6800 GB/s"}
     if dom == "vix":
-        line["note"] = ("VIX is SM-issue bound, not HBM bound: its compulsory traffic is 3 B/cell; "
-                        "see stage_work (line-of-sight samples/s) and profiles/ for issue-slot use")
+        line["note"] = ("VIX is SM-issue bound, not HBM bound: its compulsory traffic is 3 B/cell "
+                        "and ncu shows 92.7% issue-active cycles (profiles/vix_kernel_c2_2048.md); "
+                        "traffic = ncu DRAM bytes of the 2048^2 capture scaled by cells")
     work = {"vix_targets": w["nrows"] ** 2 * w["ntests"],
             "vix_targets_per_s": w["nrows"] ** 2 * w["ntests"] / (stage_ms_mean["vix"] / 1e3),
             "site_rounds": r.site_rounds, "site_picks": r.nusedsheds,

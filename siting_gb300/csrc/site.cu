@@ -11,24 +11,29 @@
 //   * pick = lowest index with the largest area > 0; stop at area 0 or when
 //     100.0*cumarea/n^2 > 95 (after adding the pick).
 //
-// GB300 mapping: one cooperative persistent kernel of G CTAs (one per SM).
-// Candidate c is owned by CTA c % G, which keeps its true gain, area, cell and
-// used flag in shared memory and a per-32-slot max tree of the keys
-// (area << 32 | ~c).  Each round every CTA
-//   1. reads the G published CTA maxima {key, cell} and reduces them to the
-//      pick (all CTAs agree; no second barrier is needed),
-//   2. computes the pick's newly covered bits N = placed(shed_p) & ~cum into
-//      shared memory (self-check: popcount(N) must equal the pick's area),
-//   3. finds its own unused candidates within 2*roi of the pick (block
-//      rectangle of the FINDMAX geometry, stepping by G) and subtracts
-//      popcount(placed(shed_c) & N) from their gains: exact, because
-//      |V_c \ (C u N)| = |V_c \ C| - |V_c n N| when N n C is empty,
-//   4. applies the intervis gate, refreshes the touched groups of its max
-//      tree and publishes its new maximum into the other parity slot.
-// CTA 0 also ORs N (and the previous round's N) into the second coverage
-// buffer, so the buffer read in a round is never written in it; one bounded
-// barrier per round orders everything.  The initial scores (popcount of every
-// shed, 128-bit loads) stream all sheds once at HBM bandwidth.
+// GB300 mapping: one persistent kernel of G co-resident CTAs (one per SM)
+// with a bounded group barrier.  Candidate c is owned by CTA c % G, which
+// keeps its true gain, area, cell and flags in shared memory and a top-4 key
+// list per 32 slots (key = area << 32 | ~c).  A round:
+//   A. every CTA publishes its own top-4 keys; one barrier;
+//   B. every CTA merges the G lists identically and accepts the longest
+//      prefix of the global key order whose members are pairwise > 2*roi
+//      apart, up to the exactness threshold (the largest 4th key of any list:
+//      unpublished keys are below it) and the 95% stop.  A candidate > 2*roi
+//      from every earlier pick of the round keeps its key, every other key
+//      can only fall, so the prefix equals the sequential greedy's next picks;
+//   C. each CTA lists its unused candidates within 2*roi of each pick;
+//   D. and computes |V_c n V_p \ cum| for each such pair: the exact gain
+//      decrease, since the picks' new bits are disjoint;
+//   E. with intervis, a candidate of area 0 whose cell a pick covers can
+//      become eligible: each CTA finds the first prefix position it would
+//      overtake, and a second barrier takes the minimum (the round's cut);
+//   F. the picks before the cut are applied: gains fall by the summed
+//      deltas, the intervis gate is re-evaluated, and the coverage bitmap is
+//      OR-ed in place (rows spread over the CTAs).  A self-check compares each
+//      pick's count of new bits with its area.
+// The round-1 gains (popcount of every shed) come from a separate streaming
+// kernel at HBM bandwidth.
 #include <algorithm>
 #include <cmath>
 #include <cstring>
