@@ -415,20 +415,127 @@ def run_batch_workload(args):
     print(json.dumps(out))
 
 
+# The serving workload: a Poisson stream of requests, sides log-uniform in
+# [256, 4096], roi U[20,200], height U[20,300], targets U[32,128],
+# bw in {8,16,32}, nwanted = n^2/128, intervis Bernoulli(0.5), served under a
+# 150 GB HBM budget.  Each request's DEM is a window of one of six 4096^2 fBm
+# rasters (submitted with its row pitch, no copy).
+def serve_jobs(nreq, seed=5):
+    import siting_gb300 as sg
+
+    rng = np.random.default_rng(seed)
+    jobs = []
+    for _ in range(nreq):
+        n = int(np.exp(rng.uniform(np.log(256), np.log(4096))))
+        p = sg.Params(nrows=n, roi=int(rng.integers(20, 201)), height=int(rng.integers(20, 301)),
+                      ntests=int(rng.integers(32, 129)), bw=int(rng.choice([8, 16, 32])),
+                      nwanted0=max(1, n * n // 128), intervis=int(rng.random() < 0.5))
+        src = int(rng.integers(0, 6))
+        x0, y0 = (int(v) for v in rng.integers(0, 4096 - n + 1, size=2))
+        jobs.append((p, src, x0, y0))
+    return jobs
+
+
+def run_serve_workload(args):
+    """Serving loop under a Poisson arrival stream: latency percentiles and
+    throughput; the first requests are re-run alone and compared."""
+    import queue
+    import threading
+
+    import siting_gb300 as sg
+
+    jobs = serve_jobs(args.serve_requests)
+    rasters = [sg.fbm_dem(4096, 4096 * 7 + i, octaves=10, ridged_weight=0.3 * (i % 2),
+                          range_max=int(2000 + 5600 * i)).reshape(4096, 4096) for i in range(6)]
+    rng = np.random.default_rng(11)
+    gaps = rng.exponential(1.0 / args.serve_rate, size=len(jobs))
+    budget = int(args.serve_budget_gb * (1 << 30))
+    srv = sg.Server(0, hbm_budget=budget, max_batch_jobs=args.batch_jobs, reserve=True)
+    # warm-up: a few requests before the clock starts
+    for p, src, x0, y0 in jobs[:3]:
+        srv.wait(srv.submit(p, rasters[src][x0:x0 + p.nrows, y0:y0 + p.nrows]))
+    infos, refused, pending = {}, 0, []
+    q = queue.Queue()
+
+    def waiter():  # collects completions in submission order
+        while (t := q.get()) is not None:
+            infos[t.id] = srv.wait(t)[2]
+
+    th = threading.Thread(target=waiter)
+    th.start()
+    t0 = time.perf_counter()
+    due = t0
+    for (p, src, x0, y0), gap in zip(jobs, gaps):
+        due += gap
+        dt = due - time.perf_counter()
+        if dt > 0:
+            time.sleep(dt)
+        try:
+            t = srv.submit(p, rasters[src][x0:x0 + p.nrows, y0:y0 + p.nrows])
+        except sg.SitingError:
+            refused += 1
+            continue
+        pending.append(t)
+        q.put(t)
+    q.put(None)
+    th.join()
+    wall = time.perf_counter() - t0
+    st = srv.stats()
+    srv.close()
+    served = [(t, infos[t.id]) for t in pending]
+    lat = np.array([i.latency_s for _, i in served]) * 1e3
+    cells = sum(t.params.nrows ** 2 for t, _ in served)
+    span = max(i.t_done for _, i in served) - min(i.t_submit for _, i in served)
+    # bit-identity: the first requests alone through a plain context
+    ctx = sg.Context(0)
+    same = True
+    for t, _ in served[:args.serve_check]:
+        o, s_, _r = ctx.run(t.params, np.ascontiguousarray(t.dem).ravel())
+        same &= bool(np.array_equal(o, t.obs) and np.array_equal(s_, t.selected))
+    ctx.close()
+    out = {"metric": "DEM cells/s served", "value": cells / span, "unit": "cells/s",
+           "n_gpus": 1, "steps": len(served), "warmup": 3, "ms_per_step": span * 1e3 / len(served),
+           "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32/u64",
+           "data": "synthetic",
+           "config": {"workload": "serve_poisson", "requests": len(jobs),
+                      "rate_per_s": args.serve_rate, "hbm_budget_gb": args.serve_budget_gb,
+                      "max_batch_jobs": args.batch_jobs,
+                      "sides": "log-U[256,4096]", "roi": "U[20,200]", "nwanted": "n^2/128"},
+           "latency_ms": {"p50": float(np.percentile(lat, 50)), "p90": float(np.percentile(lat, 90)),
+                          "p99": float(np.percentile(lat, 99)), "max": float(lat.max())},
+           "served": len(served), "refused": refused, "wall_s": wall,
+           "requests_per_s": len(served) / span,
+           "batches": st["batches"], "mean_batch_jobs": len(served) / max(1, st["batches"]),
+           "gpu_busy_frac": st["busy_s"] / max(span, 1e-9),
+           "peak_workspace_gb": st["peak_workspace"] / (1 << 30),
+           "checked_alone": min(args.serve_check, len(served)), "bit_identical_alone": same}
+    print(json.dumps(out))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--workload", default="c2_4096", choices=sorted(WORKLOADS) + ["c3_batch"])
+    ap.add_argument("--workload", default="c2_4096",
+                    choices=sorted(WORKLOADS) + ["c3_batch", "c5_serve"])
     ap.add_argument("--cpu-sample-rows", type=int, default=2048)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--batch-jobs", type=int, default=64)
+    ap.add_argument("--serve-requests", type=int, default=2000)
+    ap.add_argument("--serve-rate", type=float, default=50.0, help="mean arrivals per second")
+    ap.add_argument("--serve-budget-gb", type=float, default=150.0)
+    ap.add_argument("--serve-check", type=int, default=8,
+                    help="requests re-run alone and compared bit for bit")
     ap.add_argument("--site-ctas", type=int, default=0,
                     help="CTAs of the SITE kernel (0 = library default)")
     args = ap.parse_args()
     rank = int(os.environ.get("RANK", "0"))
+    if args.workload == "c5_serve":
+        if args.impl == "gb300" and rank == 0:
+            run_serve_workload(args)
+        return
     if args.workload == "c3_batch":
         if args.impl == "gb300" and rank == 0:
             run_batch_workload(args)

@@ -212,6 +212,57 @@ int siting_run_batch_dev(siting_ctx *ctx, int njobs, const siting_params *params
                          uint8_t *const *d_selected, siting_result *results,
                          const siting_plan *plans);
 
+/* Device workspace siting_run_batch would take for these jobs (no device
+ * work; plans may be NULL).  No counterpart in the reference. */
+int siting_batch_workspace_bytes(siting_ctx *ctx, int njobs,
+                                 const siting_params *params,
+                                 const siting_plan *plans, size_t *bytes);
+
+/* ---- serving loop --------------------------------------------------------
+ * No counterpart in the reference (one process per DEM there).  A server
+ * owns a context and a worker thread: submitted jobs queue in arrival order;
+ * whenever the GPU is free the worker takes the longest FIFO prefix of the
+ * queue (at most max_batch_jobs) whose batch workspace fits the HBM budget
+ * and runs it as one siting_run_batch (continuous batching).  A job that
+ * alone exceeds the budget is refused at submission (SITING_ENOMEM).  The
+ * workspace stays allocated between batches; with reserve != 0 the whole
+ * budget is allocated at creation, so the serving path never allocates.
+ * Each job's results equal siting_run's on the same input. */
+typedef struct siting_server siting_server;
+
+typedef struct {
+  int status;                 /* SITING_OK or the batch's error */
+  siting_result result;       /* phase times are the batch's */
+  double t_submit, t_start, t_done; /* seconds since the server started */
+  int batch_id, batch_jobs;   /* which batch ran the job, and its size */
+  char error[160];            /* message when status != SITING_OK */
+} siting_job_info;
+
+typedef struct {
+  long long submitted, completed, refused, batches, pending;
+  size_t peak_workspace;      /* largest batch workspace run, bytes */
+  double busy_s;              /* time spent running batches */
+} siting_server_stats;
+
+/* hbm_budget in bytes (required); max_batch_jobs <= 0 means 64. */
+int siting_server_create(int device, size_t hbm_budget, int max_batch_jobs,
+                         int reserve, siting_server **out);
+/* Drains the queue, stops the worker and frees the context. */
+int siting_server_destroy(siting_server *s);
+/* Queues one job.  elevs is the host DEM with a row pitch of pitch elements
+ * (0 = nrows), so a window of a larger raster can be submitted without a
+ * copy; elevs, obs and selected (nwanted entries each) must stay valid until
+ * the job is waited for.  *ticket identifies the job. */
+int siting_server_submit(siting_server *s, const siting_params *p,
+                         const uint16_t *elevs, int pitch, int32_t *obs,
+                         uint8_t *selected, long long *ticket);
+/* Waits up to timeout_s seconds (< 0: forever) for a job.  SITING_OK and
+ * *info once it is done (the ticket is then released), SITING_ETIMEOUT if it
+ * is still queued or running, SITING_EINVAL for an unknown ticket. */
+int siting_server_wait(siting_server *s, long long ticket, double timeout_s,
+                       siting_job_info *info);
+int siting_server_stats_get(siting_server *s, siting_server_stats *st);
+
 /* ---- files (the reference's input and output formats) ------------------ */
 /* Reads exactly nrows*nrows uint16 (siting.cpp:726-730). */
 int siting_read_dem(const char *path, int nrows, uint16_t *out);

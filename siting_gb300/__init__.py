@@ -120,6 +120,18 @@ class Result:
         return Result(*(getattr(r, f) for f, _ in _ResultC._fields_))
 
 
+class _JobInfoC(C.Structure):
+    _fields_ = [("status", C.c_int), ("result", _ResultC), ("t_submit", C.c_double),
+                ("t_start", C.c_double), ("t_done", C.c_double), ("batch_id", C.c_int),
+                ("batch_jobs", C.c_int), ("error", C.c_char * 160)]
+
+
+class _ServerStatsC(C.Structure):
+    _fields_ = [("submitted", C.c_longlong), ("completed", C.c_longlong),
+                ("refused", C.c_longlong), ("batches", C.c_longlong), ("pending", C.c_longlong),
+                ("peak_workspace", C.c_size_t), ("busy_s", C.c_double)]
+
+
 _lib = None
 _P = C.c_void_p
 
@@ -162,6 +174,12 @@ def load() -> C.CDLL:
         "siting_last_site_phase_cycles": ([_P, _P, i], i),
         "siting_run_batch": ([_P, i, _P, _P, _P, _P, _P, _P], i),
         "siting_run_batch_dev": ([_P, i, _P, _P, _P, _P, _P, _P], i),
+        "siting_batch_workspace_bytes": ([_P, i, _P, _P, C.POINTER(sz)], i),
+        "siting_server_create": ([i, sz, i, i, C.POINTER(_P)], i),
+        "siting_server_destroy": ([_P], i),
+        "siting_server_submit": ([_P, C.POINTER(_ParamsC), _P, i, _P, _P, C.POINTER(ll)], i),
+        "siting_server_wait": ([_P, ll, C.c_double, C.POINTER(_JobInfoC)], i),
+        "siting_server_stats_get": ([_P, C.POINTER(_ServerStatsC)], i),
         "siting_read_dem": ([C.c_char_p, i, _P], i),
         "siting_write_observers": ([C.c_char_p, i, i, _P, _P], i),
         "siting_fbm_dem": ([_P, i, C.c_uint64, i, C.c_double, C.c_double, C.c_double,
@@ -412,3 +430,114 @@ class Context:
     def run_batch_dev(self, params, d_dems, d_obs, d_sels, plans=None):
         """Device buffers (pointers or tensors) in and out; per job Result."""
         return self._batch(self._lib.siting_run_batch_dev, params, d_dems, d_obs, d_sels, plans)
+
+    def batch_workspace_bytes(self, params, plans=None) -> int:
+        """Device workspace run_batch would take for these jobs (no device work)."""
+        nj = len(params)
+        pa = (_ParamsC * nj)(*[p.c() for p in params])
+        pl = (_PlanC * nj)(*[q.c() for q in plans]) if plans is not None else None
+        out = C.c_size_t()
+        self._check(self._lib.siting_batch_workspace_bytes(self.h, nj, pa, pl, C.byref(out)))
+        return out.value
+
+
+@dataclass
+class JobInfo:
+    """Outcome of one served job; times in seconds since the server started."""
+    status: int
+    result: Result
+    t_submit: float
+    t_start: float
+    t_done: float
+    batch_id: int
+    batch_jobs: int
+    error: str
+
+    @property
+    def latency_s(self) -> float:
+        return self.t_done - self.t_submit
+
+
+@dataclass
+class Ticket:
+    id: int
+    params: Params
+    obs: np.ndarray
+    selected: np.ndarray
+    dem: np.ndarray  # kept alive until the job is waited for
+
+
+class Server:
+    """Serving loop: continuous batching of submitted jobs under an HBM budget
+    (siting_server_* in the library; one worker thread owns the GPU)."""
+
+    def __init__(self, device: int = 0, hbm_budget: int = 8 << 30, max_batch_jobs: int = 64,
+                 reserve: bool = False):
+        self._lib = load()
+        h = _P()
+        rc = self._lib.siting_server_create(device, hbm_budget, max_batch_jobs, int(reserve),
+                                            C.byref(h))
+        if rc:
+            raise SitingError(rc, f"siting_server_create(device={device}) failed: "
+                                  f"{self._lib.siting_status_string(rc).decode()}")
+        self.h = h
+
+    def close(self):
+        if getattr(self, "h", None):
+            self._lib.siting_server_destroy(self.h)
+            self.h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        self.close()
+
+    def submit(self, p: Params, dem: np.ndarray) -> Ticket:
+        """Queues one job.  dem: uint16, either nrows*nrows contiguous or a 2-D
+        window (row stride in whole elements) of a larger raster."""
+        if dem.dtype != np.uint16:
+            raise SitingError(EINVAL, "dem must be uint16")
+        pitch = 0
+        if dem.ndim == 2:
+            if dem.strides[1] != 2 or dem.strides[0] % 2 or dem.shape != (p.nrows, p.nrows):
+                raise SitingError(EINVAL, "dem window must be nrows x nrows with unit column stride")
+            pitch = dem.strides[0] // 2
+        elif not dem.flags.c_contiguous or dem.size != p.nrows * p.nrows:
+            raise SitingError(EINVAL, "dem must hold nrows*nrows contiguous elements")
+        g = block_geometry(p.nrows, p.bw, p.nwanted0)
+        obs = np.empty(g.nwanted, np.int32)
+        sel = np.empty(g.nwanted, np.uint8)
+        pc = p.c()
+        tid = C.c_longlong()
+        rc = self._lib.siting_server_submit(self.h, C.byref(pc), dem.ctypes.data, pitch,
+                                            obs.ctypes.data, sel.ctypes.data, C.byref(tid))
+        if rc:
+            raise SitingError(rc, f"submit refused: {self._lib.siting_status_string(rc).decode()}")
+        return Ticket(tid.value, p, obs, sel, dem)
+
+    def wait(self, t: Ticket, timeout: float | None = None):
+        """(obs, selected, JobInfo) once the job is done; TimeoutError if it is
+        not done within timeout seconds."""
+        info = _JobInfoC()
+        rc = self._lib.siting_server_wait(self.h, t.id, -1.0 if timeout is None else timeout,
+                                          C.byref(info))
+        if rc == ETIMEOUT:
+            raise TimeoutError(f"job {t.id} not done within {timeout} s")
+        if rc:
+            raise SitingError(rc, f"wait({t.id}) failed")
+        ji = JobInfo(info.status, Result.of(info.result), info.t_submit, info.t_start,
+                     info.t_done, info.batch_id, info.batch_jobs, info.error.decode())
+        if ji.status:
+            raise SitingError(ji.status, ji.error)
+        return t.obs, t.selected, ji
+
+    def stats(self) -> dict:
+        st = _ServerStatsC()
+        rc = self._lib.siting_server_stats_get(self.h, C.byref(st))
+        if rc:
+            raise SitingError(rc, "stats failed")
+        return {f: getattr(st, f) for f, _ in _ServerStatsC._fields_}

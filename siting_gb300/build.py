@@ -61,7 +61,8 @@ def build(verbose: bool = False, jobs: int | None = None) -> str:
     nvcc = _nvcc()
     headers = glob.glob(os.path.join(CSRC, "*.h")) + glob.glob(os.path.join(CSRC, "*.cuh")) + \
         glob.glob(os.path.join(INCLUDE, "*.h"))
-    sources = sorted(glob.glob(os.path.join(CSRC, "*.cu")) + [os.path.join(CSRC, "demgen.cpp")])
+    sources = sorted(glob.glob(os.path.join(CSRC, "*.cu")) +
+                     [os.path.join(CSRC, f) for f in ("demgen.cpp", "serve.cpp")])
     objs, todo = [], []
     for src in sources:
         obj = os.path.join(BUILD, os.path.basename(src) + ".o")
@@ -73,7 +74,7 @@ def build(verbose: bool = False, jobs: int | None = None) -> str:
         list(ex.map(lambda c: _run(c, verbose), todo))
     if todo or _stale(LIB, objs):
         _run([nvcc] + ARCH + ["-shared", "-Xcompiler", "-fopenmp", "-o", LIB] + objs +
-             ["-lcudart", "-lgomp"], verbose)
+             ["-lcudart", "-lgomp", "-lpthread"], verbose)
     cli_src = os.path.join(CSRC, "cusite.cpp")
     if _stale(CLI, [cli_src, LIB] + headers):
         _run(["g++", "-O2", "-std=c++17", "-I" + INCLUDE, cli_src, "-o", CLI, "-L" + PKG,

@@ -11,6 +11,7 @@
 #include <numeric>
 #include <vector>
 
+#include "batch.h"
 #include "ctx.h"
 #include "kernels.h"
 #include "siting.h"
@@ -18,19 +19,6 @@
 using namespace siting;
 
 namespace {
-
-struct Job {
-  siting_params p;
-  siting_geometry g;
-  int n, pitch, nr, nwpr, G;
-  bool auto_G;  // SITE group size chosen here (not by the caller's plan)
-  size_t per;
-  VixPlan vp;
-  ShedPlan sp;
-  // workspace offsets
-  size_t o_dem, o_vix, o_obs, o_sel, o_sheds, o_tab, o_site, o_err;
-  size_t site_zero;  // bytes of the SITE scratch that start at zero
-};
 
 size_t align256(size_t b) { return (b + 255) & ~(size_t)255; }
 
@@ -46,22 +34,26 @@ bool site_fits(const Job &J, int G) {
                          J.g.blocksize) <= 220 * 1024;
 }
 
-int run_batch(siting_ctx *ctx, int njobs, const siting_params *params,
-              const uint16_t *const *elevs, bool host_io, int32_t *const *obs_out,
-              uint8_t *const *sel_out, siting_result *results, const siting_plan *plans) {
-  if (!ctx || njobs < 0 || (njobs && (!params || !elevs || !obs_out || !sel_out)))
-    return fail(ctx, SITING_EINVAL, "run_batch: null argument");
-  if (njobs == 0) return SITING_OK;
-  cudaSetDevice(ctx->device);
-  std::vector<Job> jobs(njobs);
+}  // namespace
+
+namespace siting {
+
+// Launch plan and workspace layout of a batch: pure host arithmetic (no
+// device work), so that admission control can size a batch before running it.
+int plan_batch(int sm_count, int njobs, const siting_params *params, const siting_plan *plans,
+               BatchPlan *bp, std::string *err) {
+  auto bad = [&](int j, const std::string &m) {
+    *err = "job " + std::to_string(j) + ": " + m;
+    return SITING_EINVAL;
+  };
+  std::vector<Job> &jobs = bp->jobs;
+  jobs.assign(njobs, Job{});
   size_t ws = 0, tab_bytes = 0;
   for (int j = 0; j < njobs; j++) {
     Job &J = jobs[j];
     J.p = params[j];
     std::string m;
-    if (validate(&J.p, 1, &m)) return fail(ctx, SITING_EINVAL, "job " + std::to_string(j) + ": " + m);
-    if (!elevs[j] || !obs_out[j] || !sel_out[j])
-      return fail(ctx, SITING_EINVAL, "job " + std::to_string(j) + ": null buffer");
+    if (validate(&J.p, 1, &m)) return bad(j, m);
     geometry_of(J.p.nrows, J.p.bw, J.p.nwanted0, &J.g);
     J.n = J.p.nrows;
     J.pitch = (J.n + 7) & ~7;
@@ -71,24 +63,24 @@ int run_batch(siting_ctx *ctx, int njobs, const siting_params *params,
     const siting_plan *pl = plans ? &plans[j] : nullptr;
     J.vp = vix_plan_for(J.n, J.p.roi, J.p.ntests, pl ? pl->vix_tile : 0, pl ? pl->vix_smem : -1);
     J.sp = shed_plan_for(J.p.roi, pl ? pl->shed_smem : -1);
-    J.G = (pl && pl->site_ctas > 0) ? std::min(pl->site_ctas, ctx->sm_count)
-                                     : batch_site_ctas(J.g.nwanted, ctx->sm_count);
-    if (!site_supported(J.p.roi, J.g.nwanted, J.G))
-      return fail(ctx, SITING_EINVAL, "job " + std::to_string(j) + ": beyond the SITE kernel's limits");
+    J.G = (pl && pl->site_ctas > 0) ? std::min(pl->site_ctas, sm_count)
+                                     : batch_site_ctas(J.g.nwanted, sm_count);
+    if (!site_supported(J.p.roi, J.g.nwanted, J.G)) return bad(j, "beyond the SITE kernel's limits");
     J.auto_G = !(pl && pl->site_ctas > 0);
-    if (!site_fits(J, J.G))
-      return fail(ctx, SITING_EINVAL, "job " + std::to_string(j) + ": SITE shared-memory plan too large");
+    if (!site_fits(J, J.G)) return bad(j, "SITE shared-memory plan too large");
   }
   // SITE launches: pack the groups, largest first, into waves of <= sm_count CTAs
   std::vector<int> order(njobs);
   std::iota(order.begin(), order.end(), 0);
   std::stable_sort(order.begin(), order.end(),
                    [&](int a, int b) { return jobs[a].G > jobs[b].G; });
-  std::vector<std::vector<int>> waves;
-  std::vector<int> wave_ctas;
+  std::vector<std::vector<int>> &waves = bp->waves;
+  std::vector<int> &wave_ctas = bp->wave_ctas;
+  waves.clear();
+  wave_ctas.clear();
   for (int j : order) {
     size_t w = 0;
-    while (w < waves.size() && wave_ctas[w] + jobs[j].G > ctx->sm_count) w++;
+    while (w < waves.size() && wave_ctas[w] + jobs[j].G > sm_count) w++;
     if (w == waves.size()) {
       waves.emplace_back();
       wave_ctas.push_back(0);
@@ -100,7 +92,7 @@ int run_batch(siting_ctx *ctx, int njobs, const siting_params *params,
   // its automatically planned groups in proportion to their candidates (a
   // group's rounds shorten with more CTAs), up to the single-job default
   for (size_t w = 0; w < waves.size(); w++) {
-    const int spare = ctx->sm_count - wave_ctas[w];
+    const int spare = sm_count - wave_ctas[w];
     double total = 0;
     for (int j : waves[w])
       if (jobs[j].auto_G) total += jobs[j].g.nwanted;
@@ -108,7 +100,7 @@ int run_batch(siting_ctx *ctx, int njobs, const siting_params *params,
     for (int j : waves[w]) {
       Job &J = jobs[j];
       if (!J.auto_G) continue;
-      const int cap = site_default_ctas(J.g.nwanted, ctx->sm_count);
+      const int cap = site_default_ctas(J.g.nwanted, sm_count);
       const int want = std::min(cap, J.G + (int)(spare * (J.g.nwanted / total)));
       if (want > J.G && site_supported(J.p.roi, J.g.nwanted, want) && site_fits(J, want)) {
         wave_ctas[w] += want - J.G;
@@ -135,16 +127,45 @@ int run_batch(siting_ctx *ctx, int njobs, const siting_params *params,
     J.o_err = ws;
     ws += 256;
   }
-  std::vector<size_t> o_wtab(waves.size());
+  std::vector<size_t> &o_wtab = bp->o_wtab;
+  o_wtab.assign(waves.size(), 0);
   size_t wtab_bytes = 0;
   for (size_t w = 0; w < waves.size(); w++) {
     o_wtab[w] = wtab_bytes;
     wtab_bytes += align256(site_job_table_bytes((int)waves[w].size(), wave_ctas[w]));
   }
-  const size_t o_tabs = ws;
+  bp->o_tabs = ws;
   ws += align256(tab_bytes);
-  const size_t o_wtabs = ws;
+  bp->o_wtabs = ws;
   ws += align256(wtab_bytes);
+  bp->ws = ws;
+  bp->tab_bytes = tab_bytes;
+  bp->wtab_bytes = wtab_bytes;
+  return SITING_OK;
+}
+
+int run_batch(siting_ctx *ctx, int njobs, const siting_params *params,
+              const uint16_t *const *elevs, const int *src_pitch, bool host_io,
+              int32_t *const *obs_out, uint8_t *const *sel_out, siting_result *results,
+              const siting_plan *plans) {
+  if (!ctx || njobs < 0 || (njobs && (!params || !elevs || !obs_out || !sel_out)))
+    return fail(ctx, SITING_EINVAL, "run_batch: null argument");
+  if (njobs == 0) return SITING_OK;
+  for (int j = 0; j < njobs; j++)
+    if (!elevs[j] || !obs_out[j] || !sel_out[j])
+      return fail(ctx, SITING_EINVAL, "job " + std::to_string(j) + ": null buffer");
+  cudaSetDevice(ctx->device);
+  BatchPlan plan;
+  std::string perr;
+  if (int prc = plan_batch(ctx->sm_count, njobs, params, plans, &plan, &perr))
+    return fail(ctx, prc, perr);
+  std::vector<Job> &jobs = plan.jobs;
+  const auto &waves = plan.waves;
+  const auto &wave_ctas = plan.wave_ctas;
+  const auto &o_wtab = plan.o_wtab;
+  const size_t ws = plan.ws, tab_bytes = plan.tab_bytes, wtab_bytes = plan.wtab_bytes;
+  const size_t o_tabs = plan.o_tabs, o_wtabs = plan.o_wtabs;
+  (void)wave_ctas;
 
   void *base_v;
   int rc = ws_get(ctx, kBatch, ws, &base_v);
@@ -161,9 +182,9 @@ int run_batch(siting_ctx *ctx, int njobs, const siting_params *params,
   CK(cudaEventRecord(ctx->ev[5], st));
   for (int j = 0; j < njobs; j++) {  // inputs, VIX tables, zeroed scratch
     Job &J = jobs[j];
-    if (host_io || J.n % 8 || (uintptr_t)elevs[j] % 16)
-      CK(cudaMemcpy2DAsync(base + J.o_dem, (size_t)J.pitch * 2, elevs[j], (size_t)J.n * 2,
-                           (size_t)J.n * 2, J.n,
+    const size_t sp = (size_t)(src_pitch && src_pitch[j] ? src_pitch[j] : J.n) * 2;
+    if (host_io || J.n % 8 || (uintptr_t)elevs[j] % 16 || sp != (size_t)J.n * 2)
+      CK(cudaMemcpy2DAsync(base + J.o_dem, (size_t)J.pitch * 2, elevs[j], sp, (size_t)J.n * 2, J.n,
                            host_io ? cudaMemcpyHostToDevice : cudaMemcpyDeviceToDevice, st));
     vix_fill_tables(stage + s_tabs + J.o_tab, J.p.roi, J.p.ntests);
     SiteScratch s;
@@ -176,7 +197,8 @@ int run_batch(siting_ctx *ctx, int njobs, const siting_params *params,
   CK(cudaEventRecord(ctx->ev[0], st));
   auto dem_of = [&](int j) {
     const Job &J = jobs[j];
-    const bool own = host_io || J.n % 8 || (uintptr_t)elevs[j] % 16;
+    const bool own = host_io || J.n % 8 || (uintptr_t)elevs[j] % 16 ||
+                     (src_pitch && src_pitch[j] && src_pitch[j] != J.n);
     return own ? DemView{reinterpret_cast<const uint16_t *>(base + J.o_dem), J.n, J.pitch, true}
                : DemView{elevs[j], J.n, J.n, true};
   };
@@ -275,21 +297,33 @@ int run_batch(siting_ctx *ctx, int njobs, const siting_params *params,
   return SITING_OK;
 }
 
-}  // namespace
+}  // namespace siting
 
 extern "C" {
 
 int siting_run_batch(siting_ctx *ctx, int njobs, const siting_params *params,
                      const uint16_t *const *elevs, int32_t *const *obs, uint8_t *const *selected,
                      siting_result *results, const siting_plan *plans) {
-  return run_batch(ctx, njobs, params, elevs, true, obs, selected, results, plans);
+  return run_batch(ctx, njobs, params, elevs, nullptr, true, obs, selected, results, plans);
+}
+
+int siting_batch_workspace_bytes(siting_ctx *ctx, int njobs, const siting_params *params,
+                                 const siting_plan *plans, size_t *bytes) {
+  if (!ctx || njobs < 0 || (njobs && !params) || !bytes)
+    return fail(ctx, SITING_EINVAL, "batch_workspace_bytes: null argument");
+  BatchPlan plan;
+  std::string perr;
+  if (int rc = plan_batch(ctx->sm_count, njobs, params, plans, &plan, &perr))
+    return fail(ctx, rc, perr);
+  *bytes = plan.ws;
+  return SITING_OK;
 }
 
 int siting_run_batch_dev(siting_ctx *ctx, int njobs, const siting_params *params,
                          const uint16_t *const *d_elevs, int32_t *const *d_obs,
                          uint8_t *const *d_selected, siting_result *results,
                          const siting_plan *plans) {
-  return run_batch(ctx, njobs, params, d_elevs, false, d_obs, d_selected, results, plans);
+  return run_batch(ctx, njobs, params, d_elevs, nullptr, false, d_obs, d_selected, results, plans);
 }
 
 }  // extern "C"

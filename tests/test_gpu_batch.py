@@ -76,3 +76,11 @@ def test_batch_equals_single_job_runs(ctx, native):
         o2, s2, r2 = ctx.run(p, dem)
         assert np.array_equal(obs, o2) and np.array_equal(sel, s2)
         assert (res.nusedsheds, res.cumarea) == (r2.nusedsheds, r2.cumarea)
+
+
+def test_batch_large_roi(ctx, oracle, native):
+    """roi 150-200: windows beyond shared memory take the L1 paths."""
+    jobs = _mixed_jobs(native, 3, 5, sizes=(420, 520), rois=(150, 201))
+    out = ctx.run_batch([p for p, _ in jobs], [d for _, d in jobs])
+    for (p, dem), (obs, sel, res) in zip(jobs, out):
+        _check_job(oracle, p, dem, obs, sel, res)

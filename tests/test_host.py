@@ -139,3 +139,16 @@ def test_trunc_based_round_matches_roundf():
     x = v.astype(np.float64)
     want = (np.sign(x) * np.floor(np.abs(x) + 0.5)).astype(np.int64)
     assert np.array_equal(got, want)
+
+
+def test_server_refuses_without_device(native):
+    """Without a usable GPU the serving loop reports EDEVICE instead of
+    falling back to anything else."""
+    try:
+        native.Context(0).close()
+        pytest.skip("a GPU is present")
+    except native.SitingError:
+        pass
+    with pytest.raises(native.SitingError) as e:
+        native.Server(0, hbm_budget=1 << 30)
+    assert e.value.status == native.EDEVICE
