@@ -134,6 +134,16 @@ void oracle_calc_vix(int nrows, const uint16_t *elev, int roi, int oht,
     vix[c] = vix_one((int)c, nrows, elev, roi, oht, tht, ntests);
 }
 
+/* calc_vix restricted to a list of cells (the same per-cell computation,
+ * siting.cpp:137-190): spot checks of full-size rasters. */
+void oracle_vix_cells(int nrows, const uint16_t *elev, int roi, int oht,
+                      int tht, int ntests, const int64_t *cells, int count,
+                      uint8_t *out) {
+#pragma omp parallel for schedule(dynamic, 64)
+  for (int i = 0; i < count; i++)
+    out[i] = vix_one((int)cells[i], nrows, elev, roi, oht, tht, ntests);
+}
+
 /* Number of VIX targets that land in the DEM and of LOS samples they read
  * (work accounting for the VIX roofline; same walk as los_visible). */
 void oracle_vix_work(int nrows, const uint16_t *elev, int roi, int oht,

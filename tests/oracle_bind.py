@@ -83,6 +83,8 @@ class Oracle:
             lib.oracle_union_count.restype = C.c_longlong
             lib.oracle_vix_work.argtypes = [C.c_int, _u16p, C.c_int, C.c_int, C.c_int, C.c_int,
                                             C.POINTER(C.c_longlong), C.POINTER(C.c_longlong)]
+            lib.oracle_vix_cells.argtypes = [C.c_int, _u16p, C.c_int, C.c_int, C.c_int, C.c_int,
+                                             C.c_void_p, C.c_int, _u8p]
             lib.oracle_threads.restype = C.c_int
             lib.oracle_set_threads.argtypes = [C.c_int]
         elif kind in ("reference", "reference_omp"):
@@ -114,6 +116,16 @@ class Oracle:
         dem = np.ascontiguousarray(dem, np.uint16).ravel()
         fn = self.lib.oracle_calc_vix if self.kind == "port" else self.lib.ref_calc_vix
         fn(nrows, dem, roi, oht, tht, ntests, out)
+        return out
+
+    def vix_cells(self, dem: np.ndarray, nrows: int, roi: int, oht: int, tht: int, ntests: int,
+                  cells: np.ndarray) -> np.ndarray:
+        """VIX of the listed cells only (port only)."""
+        cells = np.ascontiguousarray(cells, np.int64)
+        out = np.zeros(len(cells), np.uint8)
+        dem = np.ascontiguousarray(dem, np.uint16).ravel()
+        self.lib.oracle_vix_cells(nrows, dem, roi, oht, tht, ntests, cells.ctypes.data,
+                                  len(cells), out)
         return out
 
     def find_max(self, vix: np.ndarray, nrows: int, geo: Geometry):
