@@ -153,7 +153,7 @@ __global__ void __launch_bounds__(kSiteThreads, 1)
   __shared__ long long s_cum;
   __shared__ int s_poff[kMaxPicks + 1];
   __shared__ unsigned long long s_red[32];
-  __shared__ int s_rank[kMaxPicks];
+  __shared__ int s_rank[kMaxPicks], s_rpos[kMaxPicks];
   __shared__ unsigned char s_near[kMaxPicks];
 
   const int G = a.G, k = blockIdx.x - a.block0;
@@ -216,7 +216,9 @@ __global__ void __launch_bounds__(kSiteThreads, 1)
     const int g = mine ? __ldcg(a.gains + c) : 0;
     s_gain[s] = g;
     s_area[s] = g;
-    s_pos[s] = mine ? __ldg(a.obs + c) : 0;
+    // cells as (row << 16 | column): rows and columns are below 2^16 (n^2 fits an int)
+    const int cell = mine ? __ldg(a.obs + c) : 0;
+    s_pos[s] = ((cell / n) << 16) | (cell % n);
     s_flag[s] = mine ? 0 : kUsed;
     s_dacc[s] = 0;
     s_tag[s] = 0;
@@ -347,19 +349,20 @@ __global__ void __launch_bounds__(kSiteThreads, 1)
     }
     __syncthreads();
     for (int v = tid; v < nvalid; v += blockDim.x)
-      if (s_vrank[v] < kMaxPicks) s_rank[s_vrank[v]] = s_valid[v];
+      if (s_vrank[v] < kMaxPicks) {
+        s_rank[s_vrank[v]] = s_valid[v];
+        s_rpos[s_vrank[v]] = s_mpos[s_valid[v]];
+        s_near[s_vrank[v]] = 0;
+      }
     __syncthreads();
     const int nrank = min(nvalid, kMaxPicks);
-    if (tid < nrank) {  // usable if > 2roi from every better-ranked entry
-      const int pos = s_mpos[s_rank[tid]];
-      const int px = pos / n, py = pos - (pos / n) * n;
-      bool near = false;
-      for (int j = 0; j < tid; j++) {
-        const int q = s_mpos[s_rank[j]];
-        const int dx = q / n - px, dy = q - (q / n) * n - py;
-        near |= dx * dx + dy * dy <= lim2;
-      }
-      s_near[tid] = near;
+    // usable if > 2roi from every better-ranked entry: all pairs at once
+    for (int i = tid; i < nrank * nrank; i += blockDim.x) {
+      const int r1 = i / nrank, r0 = i - r1 * nrank;
+      if (r0 >= r1) continue;
+      const int p1 = s_rpos[r1], p0 = s_rpos[r0];
+      const int dx = (p1 >> 16) - (p0 >> 16), dy = (p1 & 0xffff) - (p0 & 0xffff);
+      if (dx * dx + dy * dy <= lim2) s_near[r1] = 1;
     }
     __syncthreads();
     if (warp == 0) {  // prefix: leading usable ranks, capped, up to the 95% stop
@@ -411,7 +414,7 @@ __global__ void __launch_bounds__(kSiteThreads, 1)
       for (int i = tid; i < m * a.pick_items; i += blockDim.x) {
         const int pi = i % m, it = i / m;
         const int pos = s_ppos[pi];
-        const int px = pos / n, py = pos - (pos / n) * n;
+        const int px = pos >> 16, py = pos & 0xffff;
         const int bxl = max(0, (int)floorf(((float)px - r2f) / a.bs) - 2);
         const int bxh = min(a.nb - 1, (int)floorf(((float)px + r2f) / a.bs) + 2);
         const int byl = max(0, (int)floorf(((float)py - r2f) / a.bs) - 2);
@@ -426,7 +429,7 @@ __global__ void __launch_bounds__(kSiteThreads, 1)
         const int s = c / G;
         if (s_flag[s] & kUsed) continue;
         const int cp = s_pos[s];
-        const int cx = cp / n, cy = cp - (cp / n) * n;
+        const int cx = cp >> 16, cy = cp & 0xffff;
         const int dx = cx - px, dy = cy - py;
         if (dx * dx + dy * dy > lim2) continue;
         const int idx = atomicAdd(&s_pcnt[pi], 1);
@@ -492,7 +495,7 @@ __global__ void __launch_bounds__(kSiteThreads, 1)
         const bool own_row = (prow % G) == k;
         if (s_pcnt[pi] == 0 && !own_row) continue;
         const int pp = s_ppos[pi];
-        const int px = pp / n, py = pp - (pp / n) * n;
+        const int px = pp >> 16, py = pp & 0xffff;
         int fwp, fbp;
         shed_align(py - roi, fwp, fbp);
         const int gr = px - roi + prow;
@@ -528,7 +531,7 @@ __global__ void __launch_bounds__(kSiteThreads, 1)
         const int pi = pr / pcap;
         const int s = s_pairslot[pr];
         const int cp = s_pos[s], pp = s_ppos[pi];
-        const int cx = cp / n, cy = cp - cx * n, px = pp / n, py = pp - px * n;
+        const int cx = cp >> 16, cy = cp & 0xffff, px = pp >> 16, py = pp & 0xffff;
         const int gr = cx - roi + r, prow = gr - (px - roi);
         if (prow < 0 || prow >= nr || gr < 0 || gr >= n) continue;
         int fwc, fbc, fwp, fbp;
@@ -570,7 +573,7 @@ __global__ void __launch_bounds__(kSiteThreads, 1)
       const int r = rem / nch, ch = rem - r * nch;
       const int s = s_pairslot[pr];
       const int cp = s_pos[s], pp = s_ppos[pi];
-      const int cx = cp / n, cy = cp - cx * n, px = pp / n, py = pp - px * n;
+      const int cx = cp >> 16, cy = cp & 0xffff, px = pp >> 16, py = pp & 0xffff;
       const int gr = cx - roi + r, prow = gr - (px - roi);
       if (prow < 0 || prow >= nr || gr < 0 || gr >= n) continue;
       int fwc, fbc, fwp, fbp;
@@ -617,7 +620,7 @@ __global__ void __launch_bounds__(kSiteThreads, 1)
         const int pi = i / (rows_mine * nb2), rem = i - pi * rows_mine * nb2;
         const int prow = k + G * (rem / nb2), j = rem % nb2;
         const int pp = s_ppos[pi];
-        const int px = pp / n, py = pp - (pp / n) * n;
+        const int px = pp >> 16, py = pp & 0xffff;
         int fwp, fbp;
         shed_align(py - roi, fwp, fbp);
         const int gr = px - roi + prow, W = fwp + j;
@@ -739,7 +742,7 @@ __global__ void __launch_bounds__(kSiteThreads, 1)
         const int pi = i / (rows_mine * nb2), rem = i - pi * rows_mine * nb2;
         const int prow = k + G * (rem / nb2), j = rem % nb2;
         const int pos = s_ppos[pi];
-        const int px = pos / n, py = pos - (pos / n) * n;
+        const int px = pos >> 16, py = pos & 0xffff;
         int fwp, fbp;
         shed_align(py - roi, fwp, fbp);
         const int gr = px - roi + prow, W = fwp + j;
