@@ -178,6 +178,9 @@ def run_gpu(args, w):
     ctx = sg.Context(local)
     if args.site_ctas:
         ctx.set_site_ctas(args.site_ctas)
+    tuned = None
+    if args.autotune:  # one-off, before the clock: plans timed on a corner of the DEM
+        tuned = ctx.autotune(p, dem, sample_rows=args.autotune_rows)
     stream = torch.cuda.ExternalStream(ctx.stream)
 
     # device-resident buffers
@@ -250,7 +253,8 @@ def run_gpu(args, w):
                    "height": w["height"], "targets": w["ntests"], "bw": w["bw"],
                    "nwanted": g.nwanted, "intervis": w["intervis"],
                    "dem": f"fbm {w['octaves']} octaves, ridged {w['ridged']}, 0-{w['range_max']}",
-                   "parallelism": f"replicas{world}", "l2": "flushed (512 MiB write) between steps"},
+                   "parallelism": f"replicas{world}", "l2": "flushed (512 MiB write) between steps",
+                   "plan": "autotuned " + str(tuned) if tuned else "library default"},
         "e2e": {"value": world * n * n / (mean_e2e / 1e3), "unit": "cells/s",
                 "ms_per_step": mean_e2e, "h2d_bytes_per_step": n * n * 2,
                 "d2h_bytes_per_step": g.nwanted * 5},
@@ -523,6 +527,9 @@ def main():
     ap.add_argument("--cpu-sample-rows", type=int, default=2048)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--batch-jobs", type=int, default=64)
+    ap.add_argument("--autotune", action="store_true",
+                    help="time the launch plans on a corner of the DEM first (siting_autotune)")
+    ap.add_argument("--autotune-rows", type=int, default=1024)
     ap.add_argument("--serve-requests", type=int, default=2000)
     ap.add_argument("--serve-rate", type=float, default=50.0, help="mean arrivals per second")
     ap.add_argument("--serve-budget-gb", type=float, default=150.0)

@@ -218,6 +218,20 @@ int siting_batch_workspace_bytes(siting_ctx *ctx, int njobs,
                                  const siting_params *params,
                                  const siting_plan *plans, size_t *bytes);
 
+/* ---- autotuner -----------------------------------------------------------
+ * No counterpart in the reference.  Times the launch plans of each stage
+ * (VIX tile 16/32/64 with the halo staged or read through L1; VIEWSHED window
+ * staged or not; SITE group size when the sample is the whole DEM) on the
+ * top-left sample_rows x sample_rows corner of the host DEM elevs (0 = 1024)
+ * with p's parameters, and keeps the fastest for (roi, ntests) in the
+ * context: later calls given no plan (siting_run*, siting_run_batch* with
+ * plans == NULL, the stage functions) use it.  *best (may be NULL) receives
+ * it.  Results never depend on the plan. */
+int siting_autotune(siting_ctx *ctx, const siting_params *p,
+                    const uint16_t *elevs, int sample_rows, siting_plan *best);
+/* Forgets every autotuned plan of the context. */
+int siting_autotune_clear(siting_ctx *ctx);
+
 /* ---- serving loop --------------------------------------------------------
  * No counterpart in the reference (one process per DEM there).  A server
  * owns a context and a worker thread: submitted jobs queue in arrival order;

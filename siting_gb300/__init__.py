@@ -175,6 +175,8 @@ def load() -> C.CDLL:
         "siting_run_batch": ([_P, i, _P, _P, _P, _P, _P, _P], i),
         "siting_run_batch_dev": ([_P, i, _P, _P, _P, _P, _P, _P], i),
         "siting_batch_workspace_bytes": ([_P, i, _P, _P, C.POINTER(sz)], i),
+        "siting_autotune": ([_P, C.POINTER(_ParamsC), _P, i, C.POINTER(_PlanC)], i),
+        "siting_autotune_clear": ([_P], i),
         "siting_server_create": ([i, sz, i, i, C.POINTER(_P)], i),
         "siting_server_destroy": ([_P], i),
         "siting_server_submit": ([_P, C.POINTER(_ParamsC), _P, i, _P, _P, C.POINTER(ll)], i),
@@ -430,6 +432,19 @@ class Context:
     def run_batch_dev(self, params, d_dems, d_obs, d_sels, plans=None):
         """Device buffers (pointers or tensors) in and out; per job Result."""
         return self._batch(self._lib.siting_run_batch_dev, params, d_dems, d_obs, d_sels, plans)
+
+    def autotune(self, p: Params, dem: np.ndarray, sample_rows: int = 1024) -> Plan:
+        """Times the stages' launch plans on a corner of dem and keeps the
+        fastest for (roi, ntests) in this context; returns it."""
+        dem = np.ascontiguousarray(dem, np.uint16).ravel()
+        pc = p.c()
+        out = _PlanC()
+        self._check(self._lib.siting_autotune(self.h, C.byref(pc), dem.ctypes.data, sample_rows,
+                                              C.byref(out)))
+        return Plan(out.vix_tile, out.vix_smem, out.shed_smem, out.site_ctas)
+
+    def autotune_clear(self):
+        self._check(self._lib.siting_autotune_clear(self.h))
 
     def batch_workspace_bytes(self, params, plans=None) -> int:
         """Device workspace run_batch would take for these jobs (no device work)."""

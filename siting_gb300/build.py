@@ -62,7 +62,7 @@ def build(verbose: bool = False, jobs: int | None = None) -> str:
     headers = glob.glob(os.path.join(CSRC, "*.h")) + glob.glob(os.path.join(CSRC, "*.cuh")) + \
         glob.glob(os.path.join(INCLUDE, "*.h"))
     sources = sorted(glob.glob(os.path.join(CSRC, "*.cu")) +
-                     [os.path.join(CSRC, f) for f in ("demgen.cpp", "serve.cpp")])
+                     [os.path.join(CSRC, f) for f in ("demgen.cpp", "serve.cpp", "tune.cpp")])
     objs, todo = [], []
     for src in sources:
         obj = os.path.join(BUILD, os.path.basename(src) + ".o")

@@ -124,6 +124,12 @@ int validate(const siting_params *p, int lib_form, std::string *msg) {
   return 0;
 }
 
+const siting_plan *tuned_plan(const siting_ctx *ctx, int roi, int ntests) {
+  for (const TunedPlan &t : ctx->tuned)
+    if (t.roi == roi && (ntests < 0 || t.ntests == ntests)) return &t.plan;
+  return nullptr;
+}
+
 }  // namespace siting
 
 namespace {
@@ -201,20 +207,26 @@ int vix_dev(siting_ctx *ctx, const DemView &dem, int roi, int oht, int tht, int 
     ctx->tab_roi = roi;
     ctx->tab_ntests = ntests;
   }
-  const VixPlan plan = vix_default_plan(dem.nrows, roi, ntests);
+  const siting_plan *tp = tuned_plan(ctx, roi, ntests);
+  const VixPlan plan = tp ? vix_plan_for(dem.nrows, roi, ntests, tp->vix_tile, tp->vix_smem)
+                          : vix_default_plan(dem.nrows, roi, ntests);
   CK(launch_vix(dem, roi, oht, tht, ntests, d_vix, tab, plan, d_err, ctx->stream));
   return SITING_OK;
 }
 
 int sheds_dev(siting_ctx *ctx, const DemView &dem, int roi, int oht, int tht, int nsheds,
               const int32_t *d_obs, uint64_t *d_sheds, int *d_err) {
-  const ShedPlan plan = shed_default_plan(roi);
+  const siting_plan *tp = tuned_plan(ctx, roi, -1);
+  const ShedPlan plan = tp ? shed_plan_for(roi, tp->shed_smem) : shed_default_plan(roi);
   CK(launch_sheds(dem, roi, oht, tht, nsheds, d_obs, d_sheds, plan, d_err, ctx->stream));
   return SITING_OK;
 }
 
-int site_ctas_for(siting_ctx *ctx, int nsheds) {
-  int G = ctx->site_ctas > 0 ? ctx->site_ctas : site_default_ctas(nsheds, ctx->sm_count);
+int site_ctas_for(siting_ctx *ctx, int roi, int nsheds) {
+  const siting_plan *tp = tuned_plan(ctx, roi, -1);
+  int G = ctx->site_ctas > 0          ? ctx->site_ctas
+          : tp && tp->site_ctas > 0   ? std::max(tp->site_ctas, (nsheds + 4095) / 4096)
+                                      : site_default_ctas(nsheds, ctx->sm_count);
   return std::min(G, ctx->sm_count);
 }
 
@@ -226,7 +238,7 @@ int site_enqueue(siting_ctx *ctx, int nrows, int roi, int intervis, int nsheds,
   if (!ctx->h_out) CK(cudaMallocHost(&ctx->h_out, 16 * sizeof(long long)));
   memset(ctx->h_out, 0, 16 * sizeof(long long));
   if (nsheds <= 0) return SITING_OK;
-  const int G = site_ctas_for(ctx, nsheds);
+  const int G = site_ctas_for(ctx, roi, nsheds);
   if (!site_supported(roi, nsheds, G))
     return fail(ctx, SITING_EINVAL, "SITE: roi or nsheds beyond the device kernel's limits");
   if (site_smem_bytes(roi, nsheds, G, nb, npb, bs) > 220 * 1024)

@@ -155,6 +155,16 @@ int run_batch(siting_ctx *ctx, int njobs, const siting_params *params,
     if (!elevs[j] || !obs_out[j] || !sel_out[j])
       return fail(ctx, SITING_EINVAL, "job " + std::to_string(j) + ": null buffer");
   cudaSetDevice(ctx->device);
+  std::vector<siting_plan> tuned;  // autotuned plans where the caller gave none
+  if (!plans && !ctx->tuned.empty()) {
+    tuned.resize(njobs);
+    for (int j = 0; j < njobs; j++) {
+      const siting_plan *tp = tuned_plan(ctx, params[j].roi, params[j].ntests);
+      tuned[j] = tp ? *tp : siting_plan{0, -1, -1, 0};
+      tuned[j].site_ctas = 0;  // SITE groups are sized by the batch's packing
+    }
+    plans = tuned.data();
+  }
   BatchPlan plan;
   std::string perr;
   if (int prc = plan_batch(ctx->sm_count, njobs, params, plans, &plan, &perr))

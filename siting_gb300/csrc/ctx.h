@@ -18,6 +18,12 @@ struct DevBuf {
 
 enum Slot { kDem, kVix, kObs, kSheds, kTables, kSite, kSel, kErr, kBatch, kNumSlots };
 
+// Launch plan measured fastest by siting_autotune for (roi, ntests).
+struct TunedPlan {
+  int roi, ntests;
+  siting_plan plan;
+};
+
 }  // namespace siting
 
 struct siting_ctx {
@@ -37,6 +43,7 @@ struct siting_ctx {
   int last_nused = 0;
   unsigned char *h_stage = nullptr;   // pinned staging for batch uploads/readouts
   size_t h_stage_cap = 0;
+  std::vector<siting::TunedPlan> tuned;  // autotuned plans, used when no plan is given
 };
 
 namespace siting {
@@ -50,6 +57,9 @@ int stage_get(siting_ctx *ctx, size_t bytes, unsigned char **out);
 bool geometry_of(int nrows, int bw, int nwanted0, siting_geometry *g);
 int validate(const siting_params *p, int lib_form, std::string *msg);
 int check_err_flags(siting_ctx *ctx, const int *h_flags, int n);
+// The autotuned plan for (roi, ntests), or for roi alone when ntests < 0
+// (the VIEWSHED and SITE plans do not depend on ntests); null if none.
+const siting_plan *tuned_plan(const siting_ctx *ctx, int roi, int ntests);
 
 }  // namespace siting
 
