@@ -158,6 +158,28 @@ def site_algorithmic_bytes(nrows, roi, obs, order, nsheds):
     return total
 
 
+def max_over_ranks(values, device):
+    """Element-wise maximum over the ranks of the initialised process group
+    (the slowest replica sets the whole job's time); unchanged on one rank."""
+    import torch
+    import torch.distributed as dist
+
+    if not (dist.is_available() and dist.is_initialized()) or dist.get_world_size() == 1:
+        return list(values)
+    t = torch.tensor(list(values), dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return t.tolist()
+
+
+def workload_config(args, w, world, nwanted):
+    """The `config` of a bench line: the workload and its parameters."""
+    return {"workload": args.workload, "nrows": w["nrows"], "roi": w["roi"],
+            "height": w["height"], "targets": w["ntests"], "bw": w["bw"], "nwanted": nwanted,
+            "intervis": w["intervis"],
+            "dem": f"fbm {w['octaves']} octaves, ridged {w['ridged']}, 0-{w['range_max']}",
+            "parallelism": f"replicas{world}", "l2": "flushed (512 MiB write) between steps"}
+
+
 def run_gpu(args, w):
     import torch
 
@@ -235,12 +257,7 @@ def run_gpu(args, w):
 
     mean_dev = sum(dev_ms) / len(dev_ms)
     mean_e2e = sum(e2e_ms) / len(e2e_ms)
-    if world > 1:
-        import torch.distributed as dist
-
-        t = torch.tensor([mean_dev, mean_e2e], device=f"cuda:{local}")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        mean_dev, mean_e2e = t.tolist()
+    mean_dev, mean_e2e = max_over_ranks([mean_dev, mean_e2e], f"cuda:{local}")
     r = stage[-1]
     stage_ms = {k: sum(getattr(x, "ms_" + k) for x in stage) / len(stage)
                 for k in ("vix", "findmax", "viewshed", "site")}
@@ -249,12 +266,8 @@ def run_gpu(args, w):
         "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": mean_dev, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32/u64", "data": "synthetic",
-        "config": {"workload": args.workload, "nrows": n, "roi": w["roi"],
-                   "height": w["height"], "targets": w["ntests"], "bw": w["bw"],
-                   "nwanted": g.nwanted, "intervis": w["intervis"],
-                   "dem": f"fbm {w['octaves']} octaves, ridged {w['ridged']}, 0-{w['range_max']}",
-                   "parallelism": f"replicas{world}", "l2": "flushed (512 MiB write) between steps",
-                   "plan": "autotuned " + str(tuned) if tuned else "library default"},
+        "config": dict(workload_config(args, w, world, g.nwanted),
+                       plan="autotuned " + str(tuned) if tuned else "library default"),
         "e2e": {"value": world * n * n / (mean_e2e / 1e3), "unit": "cells/s",
                 "ms_per_step": mean_e2e, "h2d_bytes_per_step": n * n * 2,
                 "d2h_bytes_per_step": g.nwanted * 5},
@@ -345,12 +358,24 @@ def run_reference(args, w):
     sample = full.reshape(w["nrows"], w["nrows"])[:rows, :rows].copy().ravel()
     nw = max(1, int(w["nwanted0"] * (rows / w["nrows"]) ** 2))
     times = []
-    for i in range(args.warmup + args.steps):
-        t0 = time.perf_counter()
-        orc.run(sample, rows, w["roi"], w["height"], w["ntests"], w["bw"], nw, w["intervis"])
-        dt = time.perf_counter() - t0
-        if i >= args.warmup:
-            times.append(dt)
+    # the reference's SITE prints its own progress line on stdout: keep it off
+    # the bench's single JSON line
+    sys.stdout.flush()
+    saved = os.dup(1)
+    os.dup2(2, 1)
+    try:
+        for i in range(args.warmup + args.steps):
+            t0 = time.perf_counter()
+            orc.run(sample, rows, w["roi"], w["height"], w["ntests"], w["bw"], nw, w["intervis"])
+            dt = time.perf_counter() - t0
+            if i >= args.warmup:
+                times.append(dt)
+    finally:
+        import ctypes
+
+        ctypes.CDLL(None).fflush(None)  # the C library's buffered output goes to stderr too
+        os.dup2(saved, 1)
+        os.close(saved)
     mean = sum(times) / len(times)
     cores = os.cpu_count() or 1
     return {"kind": "reference" if kind != "port" else "port", "value": rows * rows / mean,
@@ -552,12 +577,16 @@ def main():
     if args.impl == "reference":
         if rank != 0:
             return
+        import siting_gb300 as sg
+
         cb = run_reference(args, w)
+        nwanted = sg.block_geometry(w["nrows"], w["bw"], w["nwanted0"]).nwanted
         line = {"metric": METRIC, "value": cb["value"], "unit": "cells/s", "n_gpus": args.gpus,
                 "steps": args.steps, "warmup": args.warmup,
                 "ms_per_step": cb["seconds_per_step"] * 1e3, "higher_is_better": True,
                 "scaling": "weak", "vs_baseline": None, "dtype": "f32/u64", "data": "synthetic",
-                "config": {"workload": args.workload, "sample": cb["sample"]},
+                "config": dict(workload_config(args, w, args.gpus, nwanted),
+                               sample=cb["sample"]),
                 "impl": "reference",
                 "cpu_baseline": {k: cb[k] for k in ("value", "unit", "cores", "kind", "sample")},
                 "e2e": {"value": cb["value"], "unit": "cells/s", "h2d_bytes_per_step": 0,
