@@ -47,7 +47,9 @@
 namespace siting {
 namespace {
 
-constexpr int kSiteThreads = 1024;
+// 512 threads a CTA: up to 128 registers a thread, so the round's phases run
+// without register spills (1024 threads capped them at 64 and spilled)
+constexpr int kSiteThreads = 512;
 constexpr int kMaxSlots = 4096;  // candidates owned by one CTA
 constexpr int kTopK = 4;         // keys each CTA publishes per round
 constexpr int kMaxPicks = 64;    // picks accepted in one round at most
