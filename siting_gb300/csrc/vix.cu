@@ -63,10 +63,11 @@ __device__ __forceinline__ int vix_target(const Dem &dem, int obase, int n, int 
                                           int tht, float span, int ox, int oy, int oz, float foz,
                                           uint32_t r1, const float *rtab) {
   const uint32_t r2 = lcg_step(r1);
-  // (int)((2*roi+0.99999f)*r/RANDOM_MAX): the divisor is 2^31, so a multiply
-  // by 2^-31 is the same exactly-rounded result.
-  int dx = f2i(fmul(fmul(span, i2f((int)r1)), 0x1p-31f)) - roi;
-  int dy = f2i(fmul(fmul(span, i2f((int)r2)), 0x1p-31f)) - roi;
+  // (int)((2*roi+0.99999f)*r/RANDOM_MAX): the divisor is 2^31, and scaling
+  // by a power of two commutes with rounding (no overflow or underflow
+  // here), so RN(span*r)/2^31 = RN((span*2^-31)*r): span arrives pre-scaled.
+  int dx = f2i(fmul(span, i2f((int)r1))) - roi;
+  int dy = f2i(fmul(span, i2f((int)r2))) - roi;
   if (dx * dx + dy * dy > roi2) {  // fold into the circle (siting.cpp:162-166)
     dx /= 3;
     dy /= 3;
@@ -78,24 +79,23 @@ __device__ __forceinline__ int vix_target(const Dem &dem, int obase, int n, int 
   const int tz = dem.at(obase + dx * W + dy) + tht;
   const bool mx = adx >= ady;
   const int d = mx ? dx : dy, m = mx ? dy : dx, ad = mx ? adx : ady;
-  const float rr = rtab[ad];
-  const float drecip = d > 0 ? rr : -rr;
-  const float slope = fmul(i2f(m), drecip);
-  const float zslope = fmul(i2f(tz - oz), drecip);
-  // Sample offsets are id = +-1, 2, 4, ... along the major axis: scaling by a
-  // power of two is exact in FP32, so slope*id and id*zslope are carried by
-  // doubling, bit-identical to the reference's products; the sample's offset
-  // from the observer is id*(major stride) + round(slope*id)*(minor stride).
-  float sl = d > 0 ? slope : -slope;
-  float zs = d > 0 ? zslope : -zslope;
-  int moff = mx ? (d > 0 ? W : -W) : (d > 0 ? 1 : -1);
+  const float rr = rtab[ad];  // |drecip| = (float)(1.0/|d|), siting.cpp:91
+  // Sample offsets are id = +-1, 2, 4, ... along the major axis (the sign of
+  // d).  slope*id = m*drecip*id = (m*|drecip|)*|id| exactly (negation and
+  // scaling by a power of two are exact in FP32), likewise id*zslope, so both
+  // are carried by doubling from m*|drecip| and (tz-oz)*|drecip|, bit-identical
+  // to the reference's products.  The sample's offset from the observer is
+  // id*(major stride) + round(slope*id)*(minor stride).
+  float sl = fmul(i2f(m), rr);
+  float zs = fmul(i2f(tz - oz), rr);
   const int smin = mx ? 1 : W;
+  int q = obase + (mx ? (d > 0 ? W : -W) : (d > 0 ? 1 : -1));  // observer + id*(major stride)
   for (int step = 1; step < ad; step <<= 1) {
     const int off = round_i(sl);
-    if (i2f(dem.at(obase + moff + off * smin)) > fadd(foz, zs)) return 0;
+    if (i2f(dem.at(q + off * smin)) > fadd(foz, zs)) return 0;
     sl = fadd(sl, sl);
     zs = fadd(zs, zs);
-    moff *= 2;
+    q = 2 * q - obase;  // id doubles
   }
   return 1;
 }
@@ -106,7 +106,7 @@ __device__ __forceinline__ void vix_tile_work(const Dem &dem, const VixArgs &a, 
   const int T = a.tile, ncell = T * T;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
   const int cb = warp * ncell / nw, ce = (warp + 1) * ncell / nw;
-  const float span = fadd(i2f(2 * a.roi), 0.99999f);
+  const float span = fmul(fadd(i2f(2 * a.roi), 0.99999f), 0x1p-31f);  // scaled by 2^-31
   const int roi2 = a.roi * a.roi;
   int cell = cb + lane / a.ntests, t = lane % a.ntests;
   int cur = -1, acc = 0, ox = 0, oy = 0, oz = 0, obase = 0;
