@@ -101,9 +101,10 @@ __device__ __forceinline__ int vix_target(const Dem &dem, int obase, int n, int 
 }
 
 template <class Dem>
-__device__ __forceinline__ void vix_tile_work(const Dem &dem, const VixArgs &a, int tx0, int ty0,
-                                              const uint2 *jump, const float *rtab, int *cnt) {
-  const int T = a.tile, ncell = T * T;
+__device__ __forceinline__ void vix_tile_work(const Dem &dem, const VixArgs &a,
+                                              const int4 *cinfo, const uint2 *jump,
+                                              const float *rtab, int *cnt) {
+  const int ncell = a.tile * a.tile;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
   const int cb = warp * ncell / nw, ce = (warp + 1) * ncell / nw;
   const float span = fmul(fadd(i2f(2 * a.roi), 0.99999f), 0x1p-31f);  // scaled by 2^-31
@@ -114,20 +115,18 @@ __device__ __forceinline__ void vix_tile_work(const Dem &dem, const VixArgs &a, 
   float foz = 0.f;
   bool valid = false;
   while (cell < ce) {
-    if (cell != cur) {
+    if (cell != cur) {  // the lane moves on to its next cell
       if (acc) atomicAdd(&cnt[cur], acc);
       cur = cell;
       acc = 0;
-      const int lx = cell / T;
-      ox = tx0 + lx;
-      oy = ty0 + (cell - lx * T);
-      valid = ox < a.n && oy < a.n;
-      if (valid) {
-        obase = dem.base(ox, oy);
-        oz = dem.at(obase) + a.oht;
-        foz = i2f(oz);
-        seed = (uint32_t)(ox * a.n + oy);
-      }
+      const int4 ci = cinfo[cell];
+      obase = ci.x;
+      oz = ci.y;
+      foz = i2f(oz);
+      seed = (uint32_t)ci.z;
+      valid = ci.w >= 0;
+      ox = ci.w >> 16;
+      oy = ci.w & 0xffff;
     }
     if (valid) {
       const uint2 j = jump[t];
@@ -164,6 +163,9 @@ __global__ void __launch_bounds__(1024) vix_kernel(const __grid_constant__ CUten
   off += (size_t)(a.roi + 1) * 4;
   int *cnt = reinterpret_cast<int *>(sm + off);
   off += (size_t)T * T * 4;
+  off = (off + 15) & ~(size_t)15;
+  int4 *cinfo = reinterpret_cast<int4 *>(sm + off);  // per cell: base, oz, seed, row<<16|col
+  off += (size_t)T * T * 16;
   uint8_t *vtab = sm + off;
 
   if (kSmem && threadIdx.x == 0) {
@@ -180,14 +182,33 @@ __global__ void __launch_bounds__(1024) vix_kernel(const __grid_constant__ CUten
   for (int i = threadIdx.x; i < T * T; i += blockDim.x) cnt[i] = 0;
   __syncthreads();
 
+  // per-cell constants, once per tile (rows and columns are below 2^16)
+  auto fill_cells = [&](const auto &dem) {
+    for (int i = threadIdx.x; i < T * T; i += blockDim.x) {
+      const int x = tx0 + i / T, y = ty0 + i % T;
+      int4 ci = make_int4(0, 0, 0, -1);
+      if (x < a.n && y < a.n) {
+        ci.x = dem.base(x, y);
+        ci.y = dem.at(ci.x) + a.oht;
+        ci.z = x * a.n + y;  // the LCG seed is the cell index (siting.cpp:150, r = tid)
+        ci.w = (x << 16) | y;
+      }
+      cinfo[i] = ci;
+    }
+    __syncthreads();
+  };
   if (kSmem) {
     if (!mbar_wait(mbar, 0)) {
       if (threadIdx.x == 0) atomicOr(a.err, kErrTmaTimeout);
       return;
     }
-    vix_tile_work(SmemDem{halo, a.halo_w, hx0, hy0}, a, tx0, ty0, jump, rtab, cnt);
+    const SmemDem dem{halo, a.halo_w, hx0, hy0};
+    fill_cells(dem);
+    vix_tile_work(dem, a, cinfo, jump, rtab, cnt);
   } else {
-    vix_tile_work(GlobalDem{a.dem, a.pitch}, a, tx0, ty0, jump, rtab, cnt);
+    const GlobalDem dem{a.dem, a.pitch};
+    fill_cells(dem);
+    vix_tile_work(dem, a, cinfo, jump, rtab, cnt);
   }
   __syncthreads();
   for (int i = threadIdx.x; i < T * T; i += blockDim.x) {
@@ -213,7 +234,11 @@ HaloGeom halo_geom(int tile, int roi) {
 }
 
 size_t tables_tail_bytes(int tile, int roi, int ntests) {
-  return 16 + (size_t)ntests * 8 + (size_t)(roi + 1) * 4 + (size_t)tile * tile * 4 + ntests + 1;
+  // mbarrier, jump table, reciprocals, counts, then the int4 cell table
+  // (16-byte aligned: the offsets before it are multiples of 4), VIX bytes
+  size_t b = 16 + (size_t)ntests * 8 + (size_t)(roi + 1) * 4 + (size_t)tile * tile * 4;
+  b = (b + 15) & ~(size_t)15;
+  return b + (size_t)tile * tile * 16 + ntests + 1;
 }
 
 }  // namespace
