@@ -218,6 +218,15 @@ int siting_batch_workspace_bytes(siting_ctx *ctx, int njobs,
                                  const siting_params *params,
                                  const siting_plan *plans, size_t *bytes);
 
+/* ---- self-test -----------------------------------------------------------
+ * No counterpart in the reference.  Runs one of the device's bounded waits
+ * (which 0: the SITE group barrier; 1: the TMA completion mbarrier) against a
+ * condition that is never met, giving up after max_cycles clock cycles
+ * (1..2^31).  Returns SITING_ETIMEOUT when the wait expired and reported as
+ * designed; the context stays usable.  Failure detection is tested this way
+ * instead of by faulting the device. */
+int siting_selftest_wait(siting_ctx *ctx, int which, long long max_cycles);
+
 /* ---- autotuner -----------------------------------------------------------
  * No counterpart in the reference.  Times the launch plans of each stage
  * (VIX tile 16/32/64 with the halo staged or read through L1; VIEWSHED window

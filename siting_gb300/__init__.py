@@ -177,6 +177,7 @@ def load() -> C.CDLL:
         "siting_batch_workspace_bytes": ([_P, i, _P, _P, C.POINTER(sz)], i),
         "siting_autotune": ([_P, C.POINTER(_ParamsC), _P, i, C.POINTER(_PlanC)], i),
         "siting_autotune_clear": ([_P], i),
+        "siting_selftest_wait": ([_P, i, ll], i),
         "siting_server_create": ([i, sz, i, i, C.POINTER(_P)], i),
         "siting_server_destroy": ([_P], i),
         "siting_server_submit": ([_P, C.POINTER(_ParamsC), _P, i, _P, _P, C.POINTER(ll)], i),
@@ -442,6 +443,12 @@ class Context:
         self._check(self._lib.siting_autotune(self.h, C.byref(pc), dem.ctypes.data, sample_rows,
                                               C.byref(out)))
         return Plan(out.vix_tile, out.vix_smem, out.shed_smem, out.site_ctas)
+
+    def selftest_wait(self, which: int, max_cycles: int = 1 << 22) -> int:
+        """Status of a bounded device wait run against a condition never met
+        (0: SITE group barrier, 1: TMA mbarrier): ETIMEOUT when it expired as
+        designed.  Does not raise."""
+        return self._lib.siting_selftest_wait(self.h, which, max_cycles)
 
     def autotune_clear(self):
         self._check(self._lib.siting_autotune_clear(self.h))

@@ -64,7 +64,8 @@ __device__ __forceinline__ void mbar_expect_tx(uint64_t *bar, uint32_t bytes) {
 }
 
 // Waits for phase `parity` of the mbarrier; false if the bounded wait expired.
-__device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity) {
+__device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity,
+                                          long long limit = kWaitCycles) {
   const uint32_t addr = smem_u32(bar);
   const long long t0 = clock64();
   for (;;) {
@@ -77,7 +78,7 @@ __device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity) {
         : "r"(addr), "r"(parity)
         : "memory");
     if (done) return true;
-    if (clock64() - t0 > kWaitCycles) return false;
+    if (clock64() - t0 > limit) return false;
   }
 }
 
@@ -117,7 +118,8 @@ __device__ __forceinline__ void red_release_add(unsigned *p, unsigned v) {
   asm volatile("red.release.gpu.global.add.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
 }
 
-__device__ __forceinline__ bool group_sync(GroupBarrier &b, int *err, int *s_flag) {
+__device__ __forceinline__ bool group_sync(GroupBarrier &b, int *err, int *s_flag,
+                                          long long limit = kWaitCycles) {
   __syncthreads();
   b.gen++;
   if (threadIdx.x == 0) {
@@ -126,7 +128,7 @@ __device__ __forceinline__ bool group_sync(GroupBarrier &b, int *err, int *s_fla
     const unsigned target = b.gen * b.nctas;
     const long long t0 = clock64();
     while ((int)(ld_acquire_u32(&b.bar[0]) - target) < 0) {
-      if (clock64() - t0 > kWaitCycles) {
+      if (clock64() - t0 > limit) {
         atomicOr(err, kErrBarrierTimeout);
         ok = 0;
         break;

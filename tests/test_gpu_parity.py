@@ -187,3 +187,16 @@ def test_hbm_budget_refusal(native):
         with pytest.raises(native.SitingError) as e:
             c.run(p, dem)
         assert e.value.status == 2 and "budget" in e.value.message
+
+
+@pytest.mark.parametrize("which", [0, 1])
+def test_bounded_waits_expire_and_context_survives(native, which):
+    """A wait whose condition is never met gives up after its limit, the host
+    reads SITING_ETIMEOUT, and the same context then runs a job normally."""
+    p = native.Params(nrows=128, roi=10, height=20, ntests=16, bw=16, nwanted0=64)
+    dem = native.fbm_dem(128, 5)
+    with native.Context(0) as c:
+        assert c.selftest_wait(which, 1 << 22) == native.ETIMEOUT
+        obs, sel, res = c.run(p, dem)
+        obs2, sel2, _ = native.Context(0).run(p, dem)
+        assert np.array_equal(obs, obs2) and np.array_equal(sel, sel2)
