@@ -57,8 +57,10 @@ struct GlobalDem {
   __device__ __forceinline__ int at(int o) const { return __ldg(g + o); }
 };
 
-// One random target of one cell (siting.cpp:155-175 and 54-135).
-template <class Dem>
+// One random target of one cell (siting.cpp:155-175 and 54-135).  kInterior:
+// every cell of the tile is at least roi from the DEM edge, so no target can
+// fall outside it and the bounds test is dropped.
+template <bool kInterior, class Dem>
 __device__ __forceinline__ int vix_target(const Dem &dem, int obase, int n, int roi, int roi2,
                                           int tht, float span, int ox, int oy, int oz, float foz,
                                           uint32_t r1, const float *rtab) {
@@ -72,7 +74,9 @@ __device__ __forceinline__ int vix_target(const Dem &dem, int obase, int n, int 
     dx /= 3;
     dy /= 3;
   }
-  if ((unsigned)(ox + dx) >= (unsigned)n || (unsigned)(oy + dy) >= (unsigned)n) return 0;
+  if (!kInterior &&
+      ((unsigned)(ox + dx) >= (unsigned)n || (unsigned)(oy + dy) >= (unsigned)n))
+    return 0;
   const int adx = abs(dx), ady = abs(dy);
   if (adx <= 1 && ady <= 1) return 1;
   const int W = dem.stride();
@@ -100,7 +104,7 @@ __device__ __forceinline__ int vix_target(const Dem &dem, int obase, int n, int 
   return 1;
 }
 
-template <class Dem>
+template <bool kInterior, class Dem>
 __device__ __forceinline__ void vix_tile_work(const Dem &dem, const VixArgs &a,
                                               const int4 *cinfo, const uint2 *jump,
                                               const float *rtab, int *cnt) {
@@ -131,7 +135,8 @@ __device__ __forceinline__ void vix_tile_work(const Dem &dem, const VixArgs &a,
     if (valid) {
       const uint2 j = jump[t];
       const uint32_t r1 = (j.x * seed + j.y) & 0x7fffffffu;
-      acc += vix_target(dem, obase, a.n, a.roi, roi2, a.tht, span, ox, oy, oz, foz, r1, rtab);
+      acc += vix_target<kInterior>(dem, obase, a.n, a.roi, roi2, a.tht, span, ox, oy, oz, foz, r1,
+                                   rtab);
     }
     t += 32;
     while (t >= a.ntests) {
@@ -182,6 +187,9 @@ __global__ void __launch_bounds__(1024) vix_kernel(const __grid_constant__ CUten
   for (int i = threadIdx.x; i < T * T; i += blockDim.x) cnt[i] = 0;
   __syncthreads();
 
+  // targets lie within roi of their cell (after the fold, |dx|,|dy| <= roi)
+  const bool interior = tx0 >= a.roi && ty0 >= a.roi && tx0 + T + a.roi <= a.n &&
+                        ty0 + T + a.roi <= a.n;
   // per-cell constants, once per tile (rows and columns are below 2^16)
   auto fill_cells = [&](const auto &dem) {
     for (int i = threadIdx.x; i < T * T; i += blockDim.x) {
@@ -204,11 +212,17 @@ __global__ void __launch_bounds__(1024) vix_kernel(const __grid_constant__ CUten
     }
     const SmemDem dem{halo, a.halo_w, hx0, hy0};
     fill_cells(dem);
-    vix_tile_work(dem, a, cinfo, jump, rtab, cnt);
+    if (interior)
+      vix_tile_work<true>(dem, a, cinfo, jump, rtab, cnt);
+    else
+      vix_tile_work<false>(dem, a, cinfo, jump, rtab, cnt);
   } else {
     const GlobalDem dem{a.dem, a.pitch};
     fill_cells(dem);
-    vix_tile_work(dem, a, cinfo, jump, rtab, cnt);
+    if (interior)
+      vix_tile_work<true>(dem, a, cinfo, jump, rtab, cnt);
+    else
+      vix_tile_work<false>(dem, a, cinfo, jump, rtab, cnt);
   }
   __syncthreads();
   for (int i = threadIdx.x; i < T * T; i += blockDim.x) {
