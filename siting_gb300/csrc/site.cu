@@ -47,9 +47,11 @@
 namespace siting {
 namespace {
 
-// 512 threads a CTA: up to 128 registers a thread, so the round's phases run
-// without register spills (1024 threads capped them at 64 and spilled)
-constexpr int kSiteThreads = 512;
+// Threads a CTA: 512 allow 128 registers a thread (no spills) and suit jobs
+// with few candidates per CTA and narrow sheds; 1024 (64 registers, a few
+// spills) keep more items in flight for many candidates per CTA or wide
+// sheds (measured: 4096^2/roi 100 9.9 vs 10.2 ms; 16384^2/roi 200 88.8 vs 77.8 ms).
+int site_threads_for(int nslots, int roi) { return (nslots > 1024 || roi > 127) ? 1024 : 512; }
 constexpr int kMaxSlots = 4096;  // candidates owned by one CTA
 constexpr int kTopK = 4;         // keys each CTA publishes per round
 constexpr int kMaxPicks = 64;    // picks accepted in one round at most
@@ -144,7 +146,8 @@ __global__ void __launch_bounds__(256) site_score_kernel(const uint64_t *sheds, 
 // One launch runs the greedy selection of one or more jobs (DEMs): CTA b
 // belongs to job block_job[b]; each job's CTAs form their own group with
 // their own barrier, scratch and outputs.
-__global__ void __launch_bounds__(kSiteThreads, 1)
+template <int kThreads>
+__global__ void __launch_bounds__(kThreads, 1)
     site_kernel(const SiteArgs *__restrict__ jobs, const int *__restrict__ block_job) {
   extern __shared__ __align__(16) unsigned char sm[];
   __shared__ SiteArgs s_args;
@@ -1012,13 +1015,18 @@ cudaError_t launch_site_jobs(const SiteJob *jobs, int njobs, void *d_table, void
   }
   e = cudaGetLastError();
   if (e != cudaSuccess) return e;
-  e = cudaFuncSetAttribute(site_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shm);
+  int threads = 512;
+  for (int i = 0; i < njobs; i++)
+    threads = std::max(threads, site_threads_for((jobs[i].nsheds + jobs[i].nctas - 1) /
+                                                     std::max(1, jobs[i].nctas),
+                                                 jobs[i].roi));
+  const void *kern = threads == 1024 ? (const void *)site_kernel<1024> : (const void *)site_kernel<512>;
+  e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shm);
   if (e != cudaSuccess) return e;
   const SiteArgs *d_args = static_cast<const SiteArgs *>(d_table);
   const int *d_map = reinterpret_cast<const int *>(static_cast<unsigned char *>(d_table) + off);
   void *kargs[] = {&d_args, &d_map};
-  return cudaLaunchCooperativeKernel((void *)site_kernel, dim3(total), dim3(kSiteThreads), kargs,
-                                     shm, st);
+  return cudaLaunchCooperativeKernel(kern, dim3(total), dim3(threads), kargs, shm, st);
 }
 
 cudaError_t launch_site(int nrows, int roi, int intervis, int nsheds, const int32_t *obs,
