@@ -159,10 +159,9 @@ __device__ __forceinline__ void sweep_rays(const Dem &dem, const ShedArgs &a, in
   }
 }
 
-// Two variants: CTAs of at most 800 threads compiled for two resident CTAs
-// per SM (two observers' windows in flight; the per-partition register file
-// then allows 32 registers per thread), and CTAs of up to 1024 threads for
-// larger roi.
+// CTAs of at most 800 threads compiled for two resident CTAs per SM (two
+// observers' windows in flight; the per-partition register file then allows
+// 32 registers per thread).
 template <bool kSmem>
 __device__ __forceinline__ void shed_body(const CUtensorMap &map, const ShedArgs &a) {
   extern __shared__ __align__(128) unsigned char sm[];
@@ -239,11 +238,6 @@ __global__ void __launch_bounds__(800, 2)
   shed_body<kSmem>(map, a);
 }
 
-template <bool kSmem>
-__global__ void __launch_bounds__(1024)
-    shed_kernel1(const __grid_constant__ CUtensorMap map, const ShedArgs a) {
-  shed_body<kSmem>(map, a);
-}
 
 int round8(int v) { return (v + 7) & ~7; }
 
@@ -273,15 +267,18 @@ size_t shed_smem_bytes(const ShedPlan &p, int roi) {
 }
 
 ShedPlan shed_default_plan(int roi) {
-  // one ray per thread where 8*roi rays fit a CTA, else an even split
+  // one ray per thread up to 800 rays (two resident CTAs per SM at 32
+  // registers a thread), else an even split into rounds of at most 800: a
+  // single 1024-thread CTA per SM ran 1.5x slower per ray step (roi 104-128)
   const int rays = 8 * roi;
-  const int rounds = (rays + 1023) / 1024;
-  const int threads = std::min(1024, ((rays + rounds - 1) / rounds + 31) / 32 * 32);
+  const int rounds = (rays + 799) / 800;
+  const int threads = std::min(800, ((rays + rounds - 1) / rounds + 31) / 32 * 32);
   ShedPlan p{std::max(threads, 64), true};
-  // the window is staged only while two CTAs still share an SM: a ray's steps
-  // form one dependent chain, so a single CTA per SM cannot hide the
-  // shared-memory latency and the L1 path with more resident CTAs is faster
-  if (shed_smem_bytes(p, roi) > 112 * 1024) p.use_smem = false;
+  // the window is staged only while two CTAs of a full round of rays still
+  // share an SM: a ray's steps form one dependent chain, so fewer resident
+  // warps cannot hide the shared-memory latency and the L1 path, with more
+  // resident CTAs, is faster (roi > 100 split into rounds: L1)
+  if (rounds > 1 || shed_smem_bytes(p, roi) > 112 * 1024) p.use_smem = false;
   return p;
 }
 
@@ -319,18 +316,13 @@ cudaError_t launch_sheds(const DemView &dem, int roi, int oht, int tht, int nshe
   ShedPlan eff = plan;
   eff.use_smem = smem;
   const size_t shm = shed_smem_bytes(eff, roi);
-  const bool two = plan.threads <= 800;
   auto launch = [&](auto kern) -> cudaError_t {
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shm);
     if (e != cudaSuccess) return e;
     kern<<<nsheds, plan.threads, shm, st>>>(map, a);
     return cudaSuccess;
   };
-  cudaError_t e;
-  if (smem)
-    e = two ? launch(shed_kernel2<true>) : launch(shed_kernel1<true>);
-  else
-    e = two ? launch(shed_kernel2<false>) : launch(shed_kernel1<false>);
+  const cudaError_t e = smem ? launch(shed_kernel2<true>) : launch(shed_kernel2<false>);
   if (e != cudaSuccess) return e;
   return cudaGetLastError();
 }
