@@ -8,8 +8,8 @@
 // GB300 mapping: one CTA per T x T cell tile.  The tile's halo (T+2roi rows,
 // T+2roi+7 columns rounded to 8) is loaded into shared memory by TMA
 // bulk-tensor copies, so every line-of-sight sample is a shared-memory gather.
-// Warps split the tile's cells evenly and walk the flat (cell, target) space
-// 32 items at a time; the target of item (cell, t) comes from the LCG state
+// Each thread keeps one cell per pass and takes every L-th of its targets
+// (L threads a cell); the target of item (cell, t) comes from the LCG state
 // after 2t+1 steps from the seed, obtained by an affine jump-ahead table
 // instead of a serial chain.  Per-cell hit counts accumulate in shared memory
 // and become VIX bytes through a host-computed table.  When the halo does not
@@ -104,47 +104,40 @@ __device__ __forceinline__ int vix_target(const Dem &dem, int obase, int n, int 
   return 1;
 }
 
+// The tile's (cell, target) items: L = blockDim/T^2 consecutive threads share
+// a cell (T = 16: 4) and take every L-th of its targets, so a thread keeps one
+// cell for the whole pass (no per-item bookkeeping) and a warp's lanes run the
+// same number of targets; the L partial counts are summed by shuffles.
 template <bool kInterior, class Dem>
 __device__ __forceinline__ void vix_tile_work(const Dem &dem, const VixArgs &a,
                                               const int4 *cinfo, const uint2 *jump,
                                               const float *rtab, int *cnt) {
   const int ncell = a.tile * a.tile;
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
-  const int cb = warp * ncell / nw, ce = (warp + 1) * ncell / nw;
+  const int L = max(1, (int)blockDim.x / ncell);  // a power of two: tiles are 16, 32, 64
+  const int per_pass = blockDim.x / L;
   const float span = fmul(fadd(i2f(2 * a.roi), 0.99999f), 0x1p-31f);  // scaled by 2^-31
   const int roi2 = a.roi * a.roi;
-  int cell = cb + lane / a.ntests, t = lane % a.ntests;
-  int cur = -1, acc = 0, ox = 0, oy = 0, oz = 0, obase = 0;
-  uint32_t seed = 0;
-  float foz = 0.f;
-  bool valid = false;
-  while (cell < ce) {
-    if (cell != cur) {  // the lane moves on to its next cell
-      if (acc) atomicAdd(&cnt[cur], acc);
-      cur = cell;
-      acc = 0;
+  const int sub = threadIdx.x & (L - 1);
+  for (int c0 = 0; c0 < ncell; c0 += per_pass) {
+    const int cell = c0 + threadIdx.x / L;
+    int acc = 0;
+    if (cell < ncell) {
       const int4 ci = cinfo[cell];
-      obase = ci.x;
-      oz = ci.y;
-      foz = i2f(oz);
-      seed = (uint32_t)ci.z;
-      valid = ci.w >= 0;
-      ox = ci.w >> 16;
-      oy = ci.w & 0xffff;
+      if (ci.w >= 0) {
+        const int obase = ci.x, oz = ci.y, ox = ci.w >> 16, oy = ci.w & 0xffff;
+        const float foz = i2f(oz);
+        const uint32_t seed = (uint32_t)ci.z;
+        for (int t = sub; t < a.ntests; t += L) {
+          const uint2 j = jump[t];
+          const uint32_t r1 = (j.x * seed + j.y) & 0x7fffffffu;
+          acc += vix_target<kInterior>(dem, obase, a.n, a.roi, roi2, a.tht, span, ox, oy, oz, foz,
+                                       r1, rtab);
+        }
+      }
     }
-    if (valid) {
-      const uint2 j = jump[t];
-      const uint32_t r1 = (j.x * seed + j.y) & 0x7fffffffu;
-      acc += vix_target<kInterior>(dem, obase, a.n, a.roi, roi2, a.tht, span, ox, oy, oz, foz, r1,
-                                   rtab);
-    }
-    t += 32;
-    while (t >= a.ntests) {
-      t -= a.ntests;
-      cell++;
-    }
+    for (int o = 1; o < L; o <<= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+    if (sub == 0 && cell < ncell) cnt[cell] = acc;
   }
-  if (acc) atomicAdd(&cnt[cur], acc);
 }
 
 template <bool kSmem>
@@ -184,7 +177,6 @@ __global__ void __launch_bounds__(1024) vix_kernel(const __grid_constant__ CUten
     jump[i] = make_uint2(a.jump[2 * i], a.jump[2 * i + 1]);
   for (int i = threadIdx.x; i <= a.roi; i += blockDim.x) rtab[i] = a.rtab[i];
   for (int i = threadIdx.x; i <= a.ntests; i += blockDim.x) vtab[i] = a.vtab[i];
-  for (int i = threadIdx.x; i < T * T; i += blockDim.x) cnt[i] = 0;
   __syncthreads();
 
   // targets lie within roi of their cell (after the fold, |dx|,|dy| <= roi)
