@@ -284,16 +284,17 @@ size_t vix_smem_bytes(const VixPlan &p, int roi, int ntests) {
 }
 
 // Two 1024-thread CTAs share an SM when each takes at most half of its 228 KB
-// shared memory (31 registers a thread); the second CTA fills the issue slots
-// that the first leaves while its warps drain at the end of a tile.
+// shared memory (at most 32 registers a thread); the second CTA fills the
+// issue slots that the first leaves while its warps drain at the end of a tile.
 constexpr size_t kVixTwoCtaSmem = 112 * 1024;
 constexpr size_t kVixMaxSmem = 220 * 1024;
 
 VixPlan vix_default_plan(int nrows, int roi, int ntests) {
   (void)nrows;
-  // the largest tile whose halo fits two CTAs per SM; else the L1 path, where
-  // a larger halo costs nothing
-  for (int tile : {64, 32, 16}) {
+  // 32x32 tiles (one cell a thread) are fastest wherever their halo fits two
+  // CTAs per SM, then 16x16 (four threads a cell); else the L1 path, where
+  // the halo costs nothing.  64x64 tiles (four cells a thread) never won.
+  for (int tile : {32, 16}) {
     VixPlan q{tile, 1024, true};
     if (vix_smem_bytes(q, roi, ntests) <= kVixTwoCtaSmem) return q;
   }
