@@ -302,7 +302,7 @@ def stage_bytes(w, nwanted):
 # to a launch by the units it processes; VIX traffic grows with the cells,
 # VIEWSHED's with the observers.
 NCU_TRAFFIC_PER_UNIT = {
-    "c2_4096": {"vix": ("cells", 8.406272e6 / 2048 ** 2),
+    "c2_4096": {"vix": ("cells", 8.403456e6 / 2048 ** 2),
                 "viewshed": ("observers", (8.50176e6 + 55.586304e6) / 16384)},
 }
 
@@ -333,7 +333,7 @@ def roofline(out, w, state, peaks, stage_ms_mean):
             "fallback 6800 GB/s"}
     if dom == "vix":
         line["note"] = ("VIX is SM-issue bound, not HBM bound: its compulsory traffic is 3 B/cell "
-                        "and ncu shows 93.1% issue-active cycles (profiles/vix_kernel_c2_2048.md); "
+                        "and ncu shows 93.0% issue-active cycles (profiles/vix_kernel_c2_2048.md); "
                         "traffic = ncu DRAM bytes of the 2048^2 capture scaled by cells")
     work = {"vix_targets": w["nrows"] ** 2 * w["ntests"],
             "vix_targets_per_s": w["nrows"] ** 2 * w["ntests"] / (stage_ms_mean["vix"] / 1e3),
