@@ -283,7 +283,10 @@ def run_gpu(args, w):
 
 # Compulsory HBM bytes per cell / per observer of each stage (DEM read once,
 # outputs written once), the algorithmic traffic the roofline divides by time.
-def stage_bytes(w, nwanted):
+def stage_bytes(w, nwanted, site_bytes):
+    """Algorithmic HBM bytes of each stage: VIX, FINDMAX and VIEWSHED read their
+    inputs and write their outputs once; SITE's are the reference's rescoring
+    traffic (site_algorithmic_bytes)."""
     n, roi = w["nrows"], w["roi"]
     nr = 2 * roi + 1
     shed = nr * ((nr + 63) // 64) * 8
@@ -292,18 +295,29 @@ def stage_bytes(w, nwanted):
         "vix": cells * 3,                       # DEM uint16 in, VIX uint8 out
         "findmax": cells * 1 + nwanted * 4,     # VIX in, observers out
         "viewshed": cells * 2 + nwanted * (4 + shed),  # DEM + observers in, sheds out
-        "site": nwanted * shed,                 # every shed streamed once (round-1 scores)
+        "site": site_bytes,
     }
 
 
-# DRAM traffic per unit (dram__bytes_read.sum + dram__bytes_write.sum) from
-# one ncu capture of the 2048^2 case with the 4096^2 workload's parameters
-# (profiles/vix_kernel_c2_2048.md, profiles/shed_kernel2_c2_2048.md), scaled
-# to a launch by the units it processes; VIX traffic grows with the cells,
-# VIEWSHED's with the observers.
-NCU_TRAFFIC_PER_UNIT = {
-    "c2_4096": {"vix": ("cells", 8.403456e6 / 2048 ** 2),
-                "viewshed": ("observers", (8.50176e6 + 55.586304e6) / 16384)},
+# DRAM bytes per launch (dram__bytes_read.sum + dram__bytes_write.sum) from
+# ncu: SITE and VIEWSHED captured at full size (profiles/launches_c2_4096.md),
+# VIX from the 2048^2 capture of the same parameters scaled by cells
+# (profiles/vix_kernel_c2_2048.md; its traffic is the DEM read once).
+NCU_TRAFFIC = {
+    "c2_4096": {"vix": 8.403456e6 * 4, "viewshed": 34310144 + 370521600,
+                "site": 2496809216 + 11495936},
+}
+
+ROOFLINE_NOTES = {
+    "vix": "VIX is SM-issue bound, not HBM bound: its compulsory traffic is 3 B/cell and ncu shows "
+           "93.0% issue-active cycles (profiles/vix_kernel_c2_2048.md)",
+    "site": "SITE's algorithmic bytes are the reference's rescoring traffic (every rescored "
+            "candidate's shed and coverage window per pick); this kernel updates gains by "
+            "per-pick deltas and reads less (traffic), and is bound by the latency of its "
+            "dependent rounds (two group barriers each), not by HBM "
+            "(profiles/site_kernel_c2_2048.md)",
+    "viewshed": "VIEWSHED is SM-issue bound (one dependent chain per ray); its HBM traffic is "
+                "the shed output (profiles/shed_kernel2_c2_2048.md)",
 }
 
 
@@ -312,34 +326,26 @@ def roofline(out, w, state, peaks, stage_ms_mean):
     dem, d_obs, d_sel, r, ctx, g = state
     hbm = peaks.get("hbm_gbs", 6800.0)
     src = "measured" if "hbm_gbs" in peaks else "fallback"
-    sb = stage_bytes(w, g.nwanted)
+    obs = d_obs.cpu().numpy()
+    order = ctx.last_pick_order(g.nwanted)
+    site_ref_bytes = site_algorithmic_bytes(w["nrows"], w["roi"], obs, order, g.nwanted)
+    sb = stage_bytes(w, g.nwanted, site_ref_bytes)
     stages = {}
     for k, ms in stage_ms_mean.items():
         ach = sb[k] / (ms / 1e3) / 1e9
         stages[k] = {"ms": ms, "alg_bytes": sb[k], "achieved_gbs": ach, "frac": ach / hbm}
     dom = max(stage_ms_mean, key=stage_ms_mean.get)
     d = stages[dom]
-    obs = d_obs.cpu().numpy()
-    order = ctx.last_pick_order(g.nwanted)
-    site_ref_bytes = site_algorithmic_bytes(w["nrows"], w["roi"], obs, order, g.nwanted)
-    traffic = None
-    per_unit = NCU_TRAFFIC_PER_UNIT.get(out["config"]["workload"], {}).get(dom)
-    if per_unit:
-        units = w["nrows"] ** 2 if per_unit[0] == "cells" else g.nwanted
-        traffic = per_unit[1] * units
+    traffic = NCU_TRAFFIC.get(out["config"]["workload"], {}).get(dom)
     line = {"kernel": dom, "bound": "hbm", "achieved": d["achieved_gbs"], "peak": hbm,
             "unit": "GB/s", "frac": d["frac"], "traffic": traffic,
             "peak_source": f"{src} (MEASURED_PEAKS.json hbm_gbs)" if src == "measured" else
             "fallback 6800 GB/s"}
-    if dom == "vix":
-        line["note"] = ("VIX is SM-issue bound, not HBM bound: its compulsory traffic is 3 B/cell "
-                        "and ncu shows 93.0% issue-active cycles (profiles/vix_kernel_c2_2048.md); "
-                        "traffic = ncu DRAM bytes of the 2048^2 capture scaled by cells")
+    if dom in ROOFLINE_NOTES:
+        line["note"] = ROOFLINE_NOTES[dom]
     work = {"vix_targets": w["nrows"] ** 2 * w["ntests"],
             "vix_targets_per_s": w["nrows"] ** 2 * w["ntests"] / (stage_ms_mean["vix"] / 1e3),
-            "site_rounds": r.site_rounds, "site_picks": r.nusedsheds,
-            "site_reference_rescoring_bytes": site_ref_bytes,
-            "site_reference_rescoring_gbs": site_ref_bytes / (stage_ms_mean["site"] / 1e3) / 1e9}
+            "site_rounds": r.site_rounds, "site_picks": r.nusedsheds}
     return line, stages, work
 
 
