@@ -102,21 +102,7 @@ __device__ __forceinline__ int key_index(unsigned long long key) {
 }
 
 // Slot flags
-constexpr unsigned char kUsed = 1, kTaken = 2, kInel = 4;
-
-__device__ __forceinline__ unsigned long long group_key(const int *s_area,
-                                                        const unsigned char *s_flag, int g,
-                                                        int lane, int my_slots, int G, int k) {
-  const int s = g * 32 + lane;
-  unsigned long long key = 0;
-  if (s < my_slots && !(s_flag[s] & (kUsed | kTaken))) key = make_key(s_area[s], s * G + k);
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) {
-    const unsigned long long w = __shfl_xor_sync(0xffffffffu, key, o);
-    key = w > key ? w : key;
-  }
-  return key;
-}
+constexpr unsigned char kUsed = 1, kInel = 4;
 
 // Round 1 (siting.cpp:537-549 with nusedsheds == 0): the gain of every
 // candidate against an empty coverage is the popcount of its shed.  One warp
