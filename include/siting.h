@@ -201,7 +201,10 @@ int siting_run_dev(siting_ctx *ctx, const siting_params *p,
  * run concurrently in shared cooperative launches (each job's CTA group with
  * its own barrier and scratch).  elevs[j] is job j's row-major uint16 DEM on
  * the host; obs[j] and selected[j] receive nwanted entries.  plans may be
- * NULL.  Each job's results equal siting_run's on the same input. */
+ * NULL.  Each job's results equal siting_run's on the same input.  The
+ * phase times in results are the batch's: ms_vix covers VIX, FINDMAX and
+ * VIEWSHED of every job, ms_site the SITE work left after them (SITE
+ * launches overlap the later jobs' stages). */
 int siting_run_batch(siting_ctx *ctx, int njobs, const siting_params *params,
                      const uint16_t *const *elevs, int32_t *const *obs,
                      uint8_t *const *selected, siting_result *results,

@@ -390,6 +390,8 @@ int siting_ctx_destroy(siting_ctx *ctx) {
   siting_ctx_trim(ctx);
   for (auto &ev : ctx->ev)
     if (ev) cudaEventDestroy(ev);
+  for (auto &ev : ctx->wave_ev) cudaEventDestroy(ev);
+  if (ctx->stream2) cudaStreamDestroy(ctx->stream2);
   if (ctx->stream) cudaStreamDestroy(ctx->stream);
   if (ctx->h_out) cudaFreeHost(ctx->h_out);
   if (ctx->h_stage) cudaFreeHost(ctx->h_stage);

@@ -218,41 +218,50 @@ int run_batch(siting_ctx *ctx, int njobs, const siting_params *params,
   auto sel_of = [&](int j) {
     return host_io ? reinterpret_cast<uint8_t *>(base + jobs[j].o_sel) : sel_out[j];
   };
-  for (int j = 0; j < njobs; j++) {
-    const Job &J = jobs[j];
-    CK(launch_vix(dem_of(j), J.p.roi, J.p.oht, J.p.tht, J.p.ntests, base + J.o_vix,
-                  base + o_tabs + J.o_tab, J.vp, reinterpret_cast<int *>(base + J.o_err), st));
+  // VIX, FINDMAX and VIEWSHED of every job on the context's stream, in the
+  // order of the SITE launches; each SITE launch runs on a second stream as
+  // soon as its jobs' viewsheds exist, overlapping the later jobs' stages.
+  // (SITE launches wait for their peers at group barriers; the kernels they
+  // share the SMs with never wait for SITE, so the barriers always complete.)
+  if (!ctx->stream2) CK(cudaStreamCreateWithFlags(&ctx->stream2, cudaStreamNonBlocking));
+  while (ctx->wave_ev.size() < waves.size()) {
+    cudaEvent_t e;
+    CK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+    ctx->wave_ev.push_back(e);
+  }
+  cudaStream_t st2 = ctx->stream2;
+  for (size_t w = 0; w < waves.size(); w++) {
+    for (int j : waves[w]) {
+      const Job &J = jobs[j];
+      int *err = reinterpret_cast<int *>(base + J.o_err);
+      CK(launch_vix(dem_of(j), J.p.roi, J.p.oht, J.p.tht, J.p.ntests, base + J.o_vix,
+                    base + o_tabs + J.o_tab, J.vp, err, st));
+      CK(launch_findmax(base + J.o_vix, J.n, J.g.blocksize, J.g.nblocks, J.g.nwantedperblock,
+                        obs_of(j), st));
+      CK(launch_sheds(dem_of(j), J.p.roi, J.p.oht, J.p.tht, J.g.nwanted, obs_of(j),
+                      reinterpret_cast<uint64_t *>(base + J.o_sheds), J.sp, err, st));
+    }
+    CK(cudaEventRecord(ctx->wave_ev[w], st));
   }
   CK(cudaEventRecord(ctx->ev[1], st));
-  for (int j = 0; j < njobs; j++) {
-    const Job &J = jobs[j];
-    CK(launch_findmax(base + J.o_vix, J.n, J.g.blocksize, J.g.nblocks, J.g.nwantedperblock,
-                      obs_of(j), st));
-  }
-  CK(cudaEventRecord(ctx->ev[2], st));
-  for (int j = 0; j < njobs; j++) {
-    const Job &J = jobs[j];
-    CK(launch_sheds(dem_of(j), J.p.roi, J.p.oht, J.p.tht, J.g.nwanted, obs_of(j),
-                    reinterpret_cast<uint64_t *>(base + J.o_sheds), J.sp,
-                    reinterpret_cast<int *>(base + J.o_err), st));
-  }
-  CK(cudaEventRecord(ctx->ev[3], st));
   for (size_t w = 0; w < waves.size(); w++) {
+    CK(cudaStreamWaitEvent(st2, ctx->wave_ev[w], 0));
     std::vector<SiteJob> sj;
     for (int j : waves[w]) {
       const Job &J = jobs[j];
       SiteScratch s;
       site_carve_scratch(base + J.o_site, J.n, J.g.nwanted, J.G, &s);
-      CK(cudaMemsetAsync(sel_of(j), 0, J.g.nwanted, st));
+      CK(cudaMemsetAsync(sel_of(j), 0, J.g.nwanted, st2));
       sj.push_back(SiteJob{J.n, J.p.roi, J.p.intervis, J.g.nwanted, obs_of(j),
                            reinterpret_cast<const uint64_t *>(base + J.o_sheds), J.g.blocksize,
                            J.g.nblocks, J.g.nwantedperblock, sel_of(j), s, J.G,
                            reinterpret_cast<int *>(base + J.o_err)});
     }
     CK(launch_site_jobs(sj.data(), (int)sj.size(), base + o_wtabs + o_wtab[w],
-                        stage + s_wtabs + o_wtab[w], st));
+                        stage + s_wtabs + o_wtab[w], st2));
   }
-  CK(cudaEventRecord(ctx->ev[4], st));
+  CK(cudaEventRecord(ctx->ev[4], st2));
+  CK(cudaStreamWaitEvent(st, ctx->ev[4], 0));
   // outputs and per-job readback (SITE outputs and error flag)
   long long *hout = reinterpret_cast<long long *>(stage + s_out);
   for (int j = 0; j < njobs; j++) {
@@ -283,10 +292,8 @@ int run_batch(siting_ctx *ctx, int njobs, const siting_params *params,
     }
   float t[8] = {};
   cudaEventElapsedTime(&t[0], ctx->ev[5], ctx->ev[0]);
-  cudaEventElapsedTime(&t[1], ctx->ev[0], ctx->ev[1]);
-  cudaEventElapsedTime(&t[2], ctx->ev[1], ctx->ev[2]);
-  cudaEventElapsedTime(&t[3], ctx->ev[2], ctx->ev[3]);
-  cudaEventElapsedTime(&t[4], ctx->ev[3], ctx->ev[4]);
+  cudaEventElapsedTime(&t[1], ctx->ev[0], ctx->ev[1]);  // VIX, FINDMAX, VIEWSHED of all jobs
+  cudaEventElapsedTime(&t[4], ctx->ev[1], ctx->ev[4]);  // SITE after them
   cudaEventElapsedTime(&t[5], ctx->ev[6], ctx->ev[7]);
   if (results)
     for (int j = 0; j < njobs; j++) {
@@ -298,10 +305,10 @@ int run_batch(siting_ctx *ctx, int njobs, const siting_params *params,
       r.nwanted = jobs[j].g.nwanted;
       r.site_rounds = (int)hout[16 * j + 2];
       r.ms_h2d = t[0];  // batch-wide phase times
-      r.ms_vix = t[1];
-      r.ms_findmax = t[2];
-      r.ms_viewshed = t[3];
-      r.ms_site = t[4];
+      r.ms_vix = t[1];  // VIX, FINDMAX and VIEWSHED of every job (SITE overlaps them)
+      r.ms_findmax = 0.f;
+      r.ms_viewshed = 0.f;
+      r.ms_site = t[4];  // SITE after the last VIEWSHED
       r.ms_d2h = t[5];
     }
   return SITING_OK;

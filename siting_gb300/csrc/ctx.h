@@ -44,6 +44,8 @@ struct siting_ctx {
   unsigned char *h_stage = nullptr;   // pinned staging for batch uploads/readouts
   size_t h_stage_cap = 0;
   std::vector<siting::TunedPlan> tuned;  // autotuned plans, used when no plan is given
+  cudaStream_t stream2 = nullptr;         // batches: SITE launches, overlapping `stream`
+  std::vector<cudaEvent_t> wave_ev;       // batches: one per SITE launch
 };
 
 namespace siting {
