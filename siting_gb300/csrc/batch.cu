@@ -4,9 +4,10 @@
 // CTA); the greedy SITE selections, whose dependent rounds leave most SMs
 // idle when run one job at a time, run many jobs at once: the jobs' CTA
 // groups are packed into as few cooperative launches as the SM count allows,
-// largest groups first, each group with its own barrier and scratch.  One
-// workspace holds every job's buffers; results are collected after a single
-// synchronisation.
+// largest groups first, each group with its own barrier and scratch.  Each
+// such launch runs on a second stream as soon as its jobs' viewsheds exist,
+// so the selections overlap the later jobs' stages.  One workspace holds
+// every job's buffers; results are collected after a single synchronisation.
 #include <algorithm>
 #include <numeric>
 #include <vector>
