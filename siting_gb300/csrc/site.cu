@@ -874,12 +874,14 @@ void site_carve_scratch(void *base, int nrows, int nsheds, int nctas, SiteScratc
   scratch_layout(nrows, nsheds, nctas, static_cast<unsigned char *>(base), s);
 }
 
-// Up to one CTA per SM, about 100 candidates per CTA: each round's work is
-// spread widely, while small jobs keep fewer CTAs in their barriers (1000^2,
-// 10 000 candidates: 1.79 ms at 96-100 CTAs against 1.99 ms at 152).  The
-// merged top-K lists (G * kTopK keys) stay small enough to walk with one warp.
+// Up to one CTA per SM, about 100 candidates per CTA but at least 32 CTAs:
+// each round's work is spread widely, while mid-size jobs keep fewer CTAs in
+// their barriers (1000^2, 10 000 candidates: 1.79 ms at 96-100 CTAs against
+// 1.99 ms at 152; 256^2, 512 candidates: 0.34 ms at 32 CTAs, 0.43 ms at 5).
+// The merged top-K lists (G * kTopK keys) stay small enough to walk with one
+// warp.
 int site_default_ctas(int nsheds, int sm_count) {
-  int g = std::max(1, std::min(nsheds / 100, sm_count));
+  int g = std::max(1, std::min(std::max(std::min(32, nsheds), nsheds / 100), sm_count));
   g = std::max(g, (nsheds + kMaxSlots - 1) / kMaxSlots);
   return std::min(g, std::min(sm_count, 160));
 }
