@@ -292,6 +292,7 @@ __global__ void __launch_bounds__(kThreads, 1)
     if (!group_sync(gb, a.err, &s_flagv)) return;
     mark(2);
     // ---- B. merge the published lists; accept the exact prefix --------------
+#pragma unroll 2
     for (int i = tid; i < GK; i += blockDim.x) {
       const unsigned long long *src = a.topk + ((size_t)par * GK + i) * 2;
       s_mkey[i] = __ldcg(src);
@@ -684,16 +685,13 @@ __global__ void __launch_bounds__(kThreads, 1)
     }
     // every read of the coverage this round is done once all CTAs pass here
     if (!group_sync(gb, a.err, &s_flagv)) return;
-    if (a.intervis) {
-      if (warp == 0) {
-        int c = m;
-        for (int g = lane; g < G; g += 32) c = min(c, __ldcg(a.cuts + par * G + g));
+    if (tid == 0) s_mcut = m;
+    __syncthreads();
+    if (a.intervis) {  // the smallest cut of any CTA: one load per thread
+      int c = tid < G ? __ldcg(a.cuts + par * G + tid) : m;
 #pragma unroll
-        for (int o = 16; o > 0; o >>= 1) c = min(c, __shfl_xor_sync(0xffffffffu, c, o));
-        if (lane == 0) s_mcut = c;
-      }
-    } else if (tid == 0) {
-      s_mcut = m;
+      for (int o = 16; o > 0; o >>= 1) c = min(c, __shfl_xor_sync(0xffffffffu, c, o));
+      if (lane == 0 && c < m) atomicMin(&s_mcut, c);
     }
     __syncthreads();
     const int mcut = s_mcut;
