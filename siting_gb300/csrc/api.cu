@@ -244,11 +244,11 @@ int site_enqueue(siting_ctx *ctx, int nrows, int roi, int intervis, int nsheds,
   if (site_smem_bytes(roi, nsheds, G, nb, npb, bs) > 220 * 1024)
     return fail(ctx, SITING_EINVAL, "SITE: shared-memory plan exceeds 220 KB");
   void *p;
-  const size_t sb = site_scratch_bytes(nrows, nsheds, G);
+  const size_t sb = site_scratch_bytes(nrows, nsheds, G, roi);
   int rc = ws_get(ctx, kSite, sb, &p);
   if (rc) return rc;
   SiteScratch s;
-  site_carve_scratch(p, nrows, nsheds, G, &s);
+  site_carve_scratch(p, nrows, nsheds, G, roi, &s);
   // zero coverage, slots, barrier and outputs (order is written before read)
   CK(cudaMemsetAsync(p, 0, (unsigned char *)s.order - (unsigned char *)p, ctx->stream));
   CK(cudaMemsetAsync(d_selected, 0, nsheds, ctx->stream));

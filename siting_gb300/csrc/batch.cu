@@ -124,7 +124,7 @@ int plan_batch(int sm_count, int njobs, const siting_params *params, const sitin
     J.o_tab = tab_bytes;
     tab_bytes += align256(vix_table_bytes(J.p.roi, J.p.ntests));
     J.o_site = ws;
-    ws += align256(site_scratch_bytes(J.n, J.g.nwanted, J.G));
+    ws += align256(site_scratch_bytes(J.n, J.g.nwanted, J.G, J.p.roi));
     J.o_err = ws;
     ws += 256;
   }
@@ -199,7 +199,7 @@ int run_batch(siting_ctx *ctx, int njobs, const siting_params *params,
                            host_io ? cudaMemcpyHostToDevice : cudaMemcpyDeviceToDevice, st));
     vix_fill_tables(stage + s_tabs + J.o_tab, J.p.roi, J.p.ntests);
     SiteScratch s;
-    site_carve_scratch(base + J.o_site, J.n, J.g.nwanted, J.G, &s);
+    site_carve_scratch(base + J.o_site, J.n, J.g.nwanted, J.G, J.p.roi, &s);
     J.site_zero = (unsigned char *)s.order - (base + J.o_site);
     CK(cudaMemsetAsync(base + J.o_site, 0, J.site_zero, st));
     CK(cudaMemsetAsync(base + J.o_err, 0, 256, st));
@@ -251,7 +251,7 @@ int run_batch(siting_ctx *ctx, int njobs, const siting_params *params,
     for (int j : waves[w]) {
       const Job &J = jobs[j];
       SiteScratch s;
-      site_carve_scratch(base + J.o_site, J.n, J.g.nwanted, J.G, &s);
+      site_carve_scratch(base + J.o_site, J.n, J.g.nwanted, J.G, J.p.roi, &s);
       CK(cudaMemsetAsync(sel_of(j), 0, J.g.nwanted, st2));
       sj.push_back(SiteJob{J.n, J.p.roi, J.p.intervis, J.g.nwanted, obs_of(j),
                            reinterpret_cast<const uint64_t *>(base + J.o_sheds), J.g.blocksize,
@@ -268,7 +268,7 @@ int run_batch(siting_ctx *ctx, int njobs, const siting_params *params,
   for (int j = 0; j < njobs; j++) {
     const Job &J = jobs[j];
     SiteScratch s;
-    site_carve_scratch(base + J.o_site, J.n, J.g.nwanted, J.G, &s);
+    site_carve_scratch(base + J.o_site, J.n, J.g.nwanted, J.G, J.p.roi, &s);
     CK(cudaMemcpyAsync(hout + 16 * j, s.out, 3 * sizeof(long long), cudaMemcpyDeviceToHost, st));
     CK(cudaMemcpyAsync(hout + 16 * j + 8, base + J.o_err, sizeof(int), cudaMemcpyDeviceToHost,
                        st));

@@ -72,7 +72,8 @@ cudaError_t launch_sheds(const DemView &dem, int roi, int oht, int tht, int nshe
 // ---- SITE -----------------------------------------------------------------------
 // Scratch layout of one SITE job (device, carved from one allocation).
 struct SiteScratch {
-  uint64_t *cum[2];          // nrows * ceil(nrows/64) words each, zeroed before launch
+  uint64_t *cum;             // nrows * ceil(nrows/64) words, zeroed before launch
+  uint64_t *nbits;           // the round's new bits of each pick: [64][nr][nwpr+1] words
   unsigned long long *topk;  // [2][nctas][8] x {key, cell}: published top keys
   int *cuts;                 // [2][nctas]: per-CTA prefix cut (intervis)
   int *ncount;               // [2][64]: popcount of each pick's new bits (self-check)
@@ -104,8 +105,8 @@ size_t site_job_table_bytes(int njobs, int total_ctas);
 // kept unchanged until the copy has run; NULL stages through pageable memory.
 cudaError_t launch_site_jobs(const SiteJob *jobs, int njobs, void *d_table, void *h_stage,
                              cudaStream_t st);
-size_t site_scratch_bytes(int nrows, int nsheds, int nctas);
-void site_carve_scratch(void *base, int nrows, int nsheds, int nctas, SiteScratch *s);
+size_t site_scratch_bytes(int nrows, int nsheds, int nctas, int roi);
+void site_carve_scratch(void *base, int nrows, int nsheds, int nctas, int roi, SiteScratch *s);
 int site_default_ctas(int nsheds, int sm_count);
 // Smallest covered-cell count at which the reference's 95% stop test holds.
 long long site_stop_area(int nrows);

@@ -63,7 +63,9 @@ struct SiteArgs {
   const uint64_t *sheds;
   float bs;
   int nb, npb;
-  uint64_t *cum0;  // coverage bitmap, updated in place
+  uint64_t *cum0;   // coverage bitmap, updated in place
+  uint64_t *nbits;  // [kMaxPicks][nr][nwpr+1]: the round's new bits of each pick
+  int ncap_words;   // shared-memory words for a small round's new bits
   unsigned long long *topk;  // [2][G][kTopK] x {key, cell}
   int *cuts;                 // [2][G]: per-CTA cut of the round's prefix (intervis)
   int *ncount;               // [2][kMaxPicks]: popcount of each pick's new bits
@@ -74,7 +76,6 @@ struct SiteArgs {
   const int *gains;  // round-1 gains, from site_score_kernel
   int *err;
   int nslots, pick_items, pick_cap, pair_cap;
-  int ncap_words;  // shared-memory words for the round's new bits (0 = none)
   long long stop_area;  // smallest cumarea with 100.0*cumarea/n^2 > 95 (host-computed)
   int block0;           // first CTA of this job's group in the launch
 };
@@ -150,7 +151,8 @@ __global__ void __launch_bounds__(kThreads, 1)
   const int G = a.G, k = blockIdx.x - a.block0;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nwarps = blockDim.x >> 5;
   const int n = a.n, roi = a.roi, nr = 2 * roi + 1, nwpr = (nr + 63) / 64;
-  const int nch = (nwpr + 1 + 3) / 4;  // 4-word chunks of a placed row (nwpr+1 words)
+  const int nb2 = nwpr + 1;            // words of a placed row
+  const int nch = (nb2 + 3) / 4;       // 4-word chunks of a placed row
   const int cw = (n + 63) / 64;
   const size_t per = (size_t)nr * nwpr;
   const int my_slots = k < a.nsheds ? (a.nsheds - k + G - 1) / G : 0;
@@ -400,6 +402,40 @@ __global__ void __launch_bounds__(kThreads, 1)
     const int m = s_m;
     if (m == 0) break;  // the largest area is 0
 
+    // Two ways to the picks' new bits N_p = placed(p) & ~cum.  Small rounds
+    // (every pick row one thread's item) compute all rows of every pick in
+    // shared memory in each CTA; larger rounds spread the rows over the CTAs
+    // (rows k, k+G, ... of each pick), write them to a global buffer and read
+    // them after one more barrier, so each row is computed once.  The choice
+    // depends on m only, so all CTAs make it alike.
+    const bool dist = m * nr > (int)blockDim.x || nwpr > 7 ||
+                      m * nr * nb2 > a.ncap_words;
+    // ---- D1 (spread): this CTA's rows of every pick, popcounts for the
+    // self-check
+    if (dist) {
+      const int rows_mine = k < nr ? (nr - k + G - 1) / G : 0;
+      for (int i = tid; i < m * rows_mine; i += blockDim.x) {
+        const int pi = i / rows_mine, prow = k + G * (i - (i / rows_mine) * rows_mine);
+        const int pp = s_ppos[pi];
+        const int px = pp >> 16, py = pp & 0xffff;
+        int fwp, fbp;
+        shed_align(py - roi, fwp, fbp);
+        const int gr = px - roi + prow;
+        uint64_t *nrow = a.nbits + (size_t)(pi * nr + prow) * nb2;
+        const uint64_t *prw = a.sheds + (size_t)s_pk[pi] * per + (size_t)prow * nwpr;
+        int cnt = 0;
+        for (int j = 0; j < nb2; j++) {
+          const int W = fwp + j;
+          uint64_t v = 0ull;
+          if (gr >= 0 && gr < n && W >= 0 && W < cw)
+            v = placed_word(prw, j, nwpr, fbp) & ~__ldcg(cum + (size_t)gr * cw + W);
+          __stcg(nrow + j, v);
+          cnt += __popcll(v);
+        }
+        if (cnt) atomicAdd(a.ncount + par * kMaxPicks + pi, cnt);
+      }
+    }
+
     // ---- C. own unused candidates within 2*roi of each pick ------------------
     {
       const float r2f = (float)(2 * roi);
@@ -476,9 +512,7 @@ __global__ void __launch_bounds__(kThreads, 1)
     const int npair = s_npair;
     mark(5);
 
-    const int nb2 = nwpr + 1;
-    const bool n_in_smem = m * nr * nb2 <= a.ncap_words;
-    if (n_in_smem && nwpr <= 7) {
+    if (!dist) {
       // ---- D1. new bits N = placed(p) & ~cum of each pick row, in shared
       // memory (picks with own candidates nearby, or rows of this CTA's
       // self-check); one item per row, all of its loads issued together
@@ -554,73 +588,89 @@ __global__ void __launch_bounds__(kThreads, 1)
         if (d) atomicAdd(&s_pairdelta[pr], d);
       }
     } else {
-      // ---- D. (fallback) per (pair, row, 4-word chunk): |V_c n V_p \ cum| --
-    // Every load of an item is independent (pair cell, pick cell, three rows),
-    // so an item costs one memory latency.  Rows outside the overlap of the
-    // two windows are skipped.
-    for (int i = tid; i < npair * nr * nch; i += blockDim.x) {
-      const int u = i / (nr * nch), rem = i - u * nr * nch;
-      const int pr = s_plist[u];
-      const int pi = pr / pcap;
-      const int r = rem / nch, ch = rem - r * nch;
-      const int s = s_pairslot[pr];
-      const int cp = s_pos[s], pp = s_ppos[pi];
-      const int cx = cp >> 16, cy = cp & 0xffff, px = pp >> 16, py = pp & 0xffff;
-      const int gr = cx - roi + r, prow = gr - (px - roi);
-      if (prow < 0 || prow >= nr || gr < 0 || gr >= n) continue;
-      int fwc, fbc, fwp, fbp;
-      shed_align(cy - roi, fwc, fbc);
-      shed_align(py - roi, fwp, fbp);
-      const int lwc = (cy + roi) >> 6;
-      const int lo = max(max(fwc, fwp), 0), hi = min(min(lwc, fwp + nwpr), cw - 1);
-      const int W0 = lo + 4 * ch;
-      const bool own = a.intervis && r == roi;
-      if (W0 > hi && !own) continue;
-      const uint64_t *crow = a.sheds + (size_t)(s * G + k) * per + (size_t)r * nwpr;
-      const uint64_t *prw = a.sheds + (size_t)s_pk[pi] * per + (size_t)prow * nwpr;
-      const uint64_t *xr = cum + (size_t)gr * cw;
-      uint64_t cwd[5], pwd[5], xw[4];
-#pragma unroll
-      for (int u = 0; u < 5; u++) {
-        const int jc = W0 - fwc - 1 + u, jp = W0 - fwp - 1 + u;
-        cwd[u] = (jc >= 0 && jc < nwpr) ? __ldg(crow + jc) : 0ull;
-        pwd[u] = (jp >= 0 && jp < nwpr) ? __ldg(prw + jp) : 0ull;
-      }
-#pragma unroll
-      for (int u = 0; u < 4; u++) xw[u] = (W0 + u <= hi) ? __ldcg(xr + W0 + u) : ~0ull;
-      int d = 0;
-#pragma unroll
-      for (int u = 0; u < 4; u++) {
-        const uint64_t vc = (cwd[u + 1] >> fbc) | (fbc ? cwd[u] << (64 - fbc) : 0ull);
-        const uint64_t vp = (pwd[u + 1] >> fbp) | (fbp ? pwd[u] << (64 - fbp) : 0ull);
-        d += __popcll(vc & vp & ~xw[u]);
-      }
-      if (d) atomicAdd(&s_pairdelta[pr], d);
-      if (own && ch == 0) {  // the candidate's own cell: covered by the pick?
-        const int ey = cy - py + roi;
-        if (ey >= 0 && ey < nr &&
-            ((__ldg(prw + (ey >> 6)) >> (63 - (ey & 63))) & 1ull))
-          atomicOr(reinterpret_cast<unsigned *>(s_paircov + (pr & ~3)), 1u << (8 * (pr & 3)));
-      }
-    }
-    // self-check inputs: new bits of each pick over this CTA's rows, one word
-    // per item
-    {
-      const int nb2 = nwpr + 1;
-      const int rows_mine = k < nr ? (nr - k + G - 1) / G : 0;
-      for (int i = tid; i < m * rows_mine * nb2; i += blockDim.x) {
-        const int pi = i / (rows_mine * nb2), rem = i - pi * rows_mine * nb2;
-        const int prow = k + G * (rem / nb2), j = rem % nb2;
-        const int pp = s_ppos[pi];
-        const int px = pp >> 16, py = pp & 0xffff;
-        int fwp, fbp;
+    // every CTA's rows of N are written
+    if (!group_sync(gb, a.err, &s_flagv)) return;
+    if (nwpr <= 7) {
+      // ---- D2. per (pair, row): popcount(placed(c) & N), loads issued together
+      for (int it = tid; it < npair * nr; it += blockDim.x) {
+        const int u = it / nr, r = it - u * nr;
+        const int pr = s_plist[u];
+        const int pi = pr / pcap;
+        const int s = s_pairslot[pr];
+        const int cp = s_pos[s], pp = s_ppos[pi];
+        const int cx = cp >> 16, cy = cp & 0xffff, px = pp >> 16, py = pp & 0xffff;
+        const int gr = cx - roi + r, prow = gr - (px - roi);
+        if (prow < 0 || prow >= nr || gr < 0 || gr >= n) continue;
+        int fwc, fbc, fwp, fbp;
+        shed_align(cy - roi, fwc, fbc);
         shed_align(py - roi, fwp, fbp);
-        const int gr = px - roi + prow, W = fwp + j;
-        if (gr < 0 || gr >= n || W < 0 || W >= cw) continue;
-        const uint64_t v =
-            placed_word(a.sheds + (size_t)s_pk[pi] * per + (size_t)prow * nwpr, j, nwpr, fbp) &
-            ~__ldcg(cum + (size_t)gr * cw + W);
-        if (v) atomicAdd(a.ncount + par * kMaxPicks + pi, __popcll(v));
+        const uint64_t *nrow = a.nbits + (size_t)(pi * nr + prow) * nb2;
+        if (a.intervis && r == roi) {  // own cell: newly covered by the pick?
+          const int j = (cy >> 6) - fwp;
+          if (j >= 0 && j < nb2 && ((__ldcg(nrow + j) >> (63 - (cy & 63))) & 1ull))
+            atomicOr(reinterpret_cast<unsigned *>(s_paircov + (pr & ~3)), 1u << (8 * (pr & 3)));
+        }
+        const int lo = max(max(fwc, fwp), 0);
+        const int hi = min(min((cy + roi) >> 6, fwp + nwpr), cw - 1);
+        if (lo > hi) continue;
+        const uint64_t *crow = a.sheds + (size_t)(s * G + k) * per + (size_t)r * nwpr;
+        uint64_t w[8], x[8];
+#pragma unroll
+        for (int q = 0; q < 8; q++) {
+          w[q] = q < nwpr ? __ldg(crow + q) : 0ull;
+          const int W = fwc + q;  // c's placed word q lands at column word fwc+q
+          x[q] = (q < nb2 && W >= lo && W <= hi) ? __ldcg(nrow + (W - fwp)) : 0ull;
+        }
+        int d = 0;
+#pragma unroll
+        for (int q = 0; q < 8; q++) {
+          if (q >= nb2) break;
+          const uint64_t vc = (w[q] >> fbc) | ((q > 0 && fbc) ? w[q - 1] << (64 - fbc) : 0ull);
+          d += __popcll(vc & x[q]);
+        }
+        if (d) atomicAdd(&s_pairdelta[pr], d);
+      }
+    } else {
+      // ---- D2 for wide sheds: per (pair, row, 4-word chunk)
+      for (int i = tid; i < npair * nr * nch; i += blockDim.x) {
+        const int u = i / (nr * nch), rem = i - u * nr * nch;
+        const int pr = s_plist[u];
+        const int pi = pr / pcap;
+        const int r = rem / nch, ch = rem - r * nch;
+        const int s = s_pairslot[pr];
+        const int cp = s_pos[s], pp = s_ppos[pi];
+        const int cx = cp >> 16, cy = cp & 0xffff, px = pp >> 16, py = pp & 0xffff;
+        const int gr = cx - roi + r, prow = gr - (px - roi);
+        if (prow < 0 || prow >= nr || gr < 0 || gr >= n) continue;
+        int fwc, fbc, fwp, fbp;
+        shed_align(cy - roi, fwc, fbc);
+        shed_align(py - roi, fwp, fbp);
+        const uint64_t *nrow = a.nbits + (size_t)(pi * nr + prow) * nb2;
+        if (a.intervis && r == roi && ch == 0) {  // own cell: newly covered by the pick?
+          const int j = (cy >> 6) - fwp;
+          if (j >= 0 && j < nb2 && ((__ldcg(nrow + j) >> (63 - (cy & 63))) & 1ull))
+            atomicOr(reinterpret_cast<unsigned *>(s_paircov + (pr & ~3)), 1u << (8 * (pr & 3)));
+        }
+        const int lwc = (cy + roi) >> 6;
+        const int lo = max(max(fwc, fwp), 0), hi = min(min(lwc, fwp + nwpr), cw - 1);
+        const int W0 = lo + 4 * ch;
+        if (W0 > hi) continue;
+        const uint64_t *crow = a.sheds + (size_t)(s * G + k) * per + (size_t)r * nwpr;
+        uint64_t cwd[5], xw[4];
+#pragma unroll
+        for (int t = 0; t < 5; t++) {
+          const int jc = W0 - fwc - 1 + t;
+          cwd[t] = (jc >= 0 && jc < nwpr) ? __ldg(crow + jc) : 0ull;
+        }
+#pragma unroll
+        for (int t = 0; t < 4; t++) xw[t] = (W0 + t <= hi) ? __ldcg(nrow + (W0 + t - fwp)) : 0ull;
+        int d = 0;
+#pragma unroll
+        for (int t = 0; t < 4; t++) {
+          const uint64_t vc = (cwd[t + 1] >> fbc) | (fbc ? cwd[t] << (64 - fbc) : 0ull);
+          d += __popcll(vc & xw[t]);
+        }
+        if (d) atomicAdd(&s_pairdelta[pr], d);
       }
     }
     }
@@ -725,7 +775,6 @@ __global__ void __launch_bounds__(kThreads, 1)
     }
     // coverage: OR this CTA's rows of the accepted picks' placed sheds
     {
-      const int nb2 = nwpr + 1;
       const int rows_mine = k < nr ? (nr - k + G - 1) / G : 0;
       for (int i = tid; i < mcut * rows_mine * nb2; i += blockDim.x) {
         const int pi = i / (rows_mine * nb2), rem = i - pi * rows_mine * nb2;
@@ -827,7 +876,8 @@ long long site_stop_area(int nrows) {
 
 namespace {
 
-size_t scratch_layout(int nrows, int nsheds, int nctas, unsigned char *base, SiteScratch *s) {
+size_t scratch_layout(int nrows, int nsheds, int nctas, int roi, unsigned char *base,
+                      SiteScratch *s) {
   const size_t cw = (size_t)(nrows + 63) / 64;
   size_t off = 0;
   auto take = [&](size_t bytes) {
@@ -835,8 +885,8 @@ size_t scratch_layout(int nrows, int nsheds, int nctas, unsigned char *base, Sit
     off += (bytes + 255) & ~(size_t)255;
     return q;
   };
+  // zeroed before a launch: everything up to `order`
   unsigned char *c0 = take((size_t)nrows * cw * 8);
-  unsigned char *c1 = take((size_t)nrows * cw * 8);
   unsigned char *tk = take((size_t)2 * nctas * kTopK * 2 * 8);
   unsigned char *cu = take((size_t)2 * nctas * 4);
   unsigned char *nc = take((size_t)2 * kMaxPicks * 4);
@@ -844,10 +894,12 @@ size_t scratch_layout(int nrows, int nsheds, int nctas, unsigned char *base, Sit
   unsigned char *ou = take(128);
   unsigned char *od = take((size_t)nsheds * 4);
   unsigned char *gn = take((size_t)nsheds * 4);
+  const size_t nr = 2 * (size_t)roi + 1;  // every row is written before it is read
+  unsigned char *nb = take((size_t)kMaxPicks * nr * ((nr + 63) / 64 + 1) * 8);
   unsigned char *tb = take(site_job_table_bytes(1, nctas));
   if (s) {
-    s->cum[0] = reinterpret_cast<uint64_t *>(c0);
-    s->cum[1] = reinterpret_cast<uint64_t *>(c1);
+    s->cum = reinterpret_cast<uint64_t *>(c0);
+    s->nbits = reinterpret_cast<uint64_t *>(nb);
     s->topk = reinterpret_cast<unsigned long long *>(tk);
     s->cuts = reinterpret_cast<int *>(cu);
     s->ncount = reinterpret_cast<int *>(nc);
@@ -864,12 +916,12 @@ size_t round16(size_t b) { return (b + 15) & ~(size_t)15; }
 
 }  // namespace
 
-size_t site_scratch_bytes(int nrows, int nsheds, int nctas) {
-  return scratch_layout(nrows, nsheds, nctas, nullptr, nullptr);
+size_t site_scratch_bytes(int nrows, int nsheds, int nctas, int roi) {
+  return scratch_layout(nrows, nsheds, nctas, roi, nullptr, nullptr);
 }
 
-void site_carve_scratch(void *base, int nrows, int nsheds, int nctas, SiteScratch *s) {
-  scratch_layout(nrows, nsheds, nctas, static_cast<unsigned char *>(base), s);
+void site_carve_scratch(void *base, int nrows, int nsheds, int nctas, int roi, SiteScratch *s) {
+  scratch_layout(nrows, nsheds, nctas, roi, static_cast<unsigned char *>(base), s);
 }
 
 // Up to one CTA per SM, about 100 candidates per CTA but at least 32 CTAs:
@@ -902,15 +954,17 @@ size_t site_smem_base(int roi, int nsheds, int nctas, int nblocks, int npb, floa
   return b;
 }
 
+}  // namespace
+
+// Shared words for the new bits of a small round (the spread path takes the
+// rest): up to 32 KB, within the 220 KB plan.
 constexpr size_t kSiteSmemPlan = 220 * 1024;
-constexpr int kMaxNWords = 16384;  // 128 KB of new bits: ~16 picks at roi=100
+constexpr int kMaxNWords = 4096;
 
 int site_ncap_words(size_t base) {
   if (base >= kSiteSmemPlan) return 0;
   return (int)std::min<size_t>(kMaxNWords, (kSiteSmemPlan - base) / 8 / 2 * 2);
 }
-
-}  // namespace
 
 size_t site_smem_bytes(int roi, int nsheds, int nctas, int nblocks, int npb, float blocksize) {
   const size_t base = site_smem_base(roi, nsheds, nctas, nblocks, npb, blocksize);
@@ -936,7 +990,10 @@ SiteArgs make_site_args(const SiteJob &j, int block0) {
   a.bs = j.blocksize;
   a.nb = j.nblocks;
   a.npb = j.npb;
-  a.cum0 = j.scratch.cum[0];
+  a.cum0 = j.scratch.cum;
+  a.nbits = j.scratch.nbits;
+  a.ncap_words =
+      site_ncap_words(site_smem_base(j.roi, j.nsheds, j.nctas, j.nblocks, j.npb, j.blocksize));
   a.topk = j.scratch.topk;
   a.cuts = j.scratch.cuts;
   a.ncount = j.scratch.ncount;
@@ -951,8 +1008,6 @@ SiteArgs make_site_args(const SiteJob &j, int block0) {
   a.pick_items = pb.items;
   a.pick_cap = pb.cap;
   a.pair_cap = site_pair_cap(pb);
-  a.ncap_words =
-      site_ncap_words(site_smem_base(j.roi, j.nsheds, j.nctas, j.nblocks, j.npb, j.blocksize));
   a.stop_area = site_stop_area(j.nrows);
   a.block0 = block0;
   return a;
@@ -1098,14 +1153,14 @@ extern "C" int siting_site_it_noalloc(int nrows, int roi, int intervis, int nshe
   // candidates are taken in any order: one block row holding them all
   const float bs = (float)nrows;
   if (site_smem_bytes(roi, nsheds, G, 1, nsheds, bs) > 220 * 1024) return SITING_EINVAL;
-  const size_t need = site_scratch_bytes(nrows, nsheds, G) + 256;  // + error flag
+  const size_t need = site_scratch_bytes(nrows, nsheds, G, roi) + 256;  // + error flag
   if (need > kNoAllocScratchBytes) return SITING_ENOMEM;  // beyond the 16 MiB array
   void *base = nullptr;
   int rc = noalloc_scratch(dev, &base);
   if (rc) return rc;
   cudaStream_t st = static_cast<cudaStream_t>(stream);
   SiteScratch s;
-  site_carve_scratch(base, nrows, nsheds, G, &s);
+  site_carve_scratch(base, nrows, nsheds, G, roi, &s);
   int *d_err = reinterpret_cast<int *>(static_cast<unsigned char *>(base) + need - 256);
   // zero coverage, key lists, cuts, self-check counters, barrier and outputs
   if (cudaMemsetAsync(base, 0, (unsigned char *)s.order - (unsigned char *)base, st) != cudaSuccess ||

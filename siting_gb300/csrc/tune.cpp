@@ -136,10 +136,10 @@ extern "C" int siting_autotune(siting_ctx *ctx, const siting_params *p, const ui
               220 * 1024)
         continue;
       void *sp;
-      const size_t sb = site_scratch_bytes(n, g.nwanted, G);
+      const size_t sb = site_scratch_bytes(n, g.nwanted, G, p->roi);
       if ((rc = ws_get(ctx, kSite, sb, &sp))) return rc;
       SiteScratch s;
-      site_carve_scratch(sp, n, g.nwanted, G, &s);
+      site_carve_scratch(sp, n, g.nwanted, G, p->roi, &s);
       float t;
       rc = time_ms(ctx, [&] {
         cudaError_t e = cudaMemsetAsync(sp, 0, (unsigned char *)s.order - (unsigned char *)sp, st);
