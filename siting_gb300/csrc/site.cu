@@ -23,8 +23,11 @@
 //      from every earlier pick of the round keeps its key, every other key
 //      can only fall, so the prefix equals the sequential greedy's next picks;
 //   C. each CTA lists its unused candidates within 2*roi of each pick;
-//   D. and computes |V_c n V_p \ cum| for each such pair: the exact gain
-//      decrease, since the picks' new bits are disjoint;
+//   D. and computes |V_c n N_p| for each such pair, N_p = placed(V_p) \ cum
+//      the pick's new bits: the exact gain decrease, since the picks' new
+//      bits are disjoint.  Small rounds compute N in every CTA's shared
+//      memory; larger ones spread its rows over the CTAs (a global buffer
+//      read after one more barrier);
 //   E. with intervis, a candidate of area 0 whose cell a pick covers can
 //      become eligible: each CTA finds the first prefix position it would
 //      overtake, and a second barrier takes the minimum (the round's cut);
