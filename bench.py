@@ -304,8 +304,8 @@ def stage_bytes(w, nwanted, site_bytes):
 # VIX from the 2048^2 capture of the same parameters scaled by cells
 # (profiles/vix_kernel_c2_2048.md; its traffic is the DEM read once).
 NCU_TRAFFIC = {
-    "c2_4096": {"vix": 8.403456e6 * 4, "viewshed": 34310144 + 370521600,
-                "site": 2496809216 + 11495936},
+    "c2_4096": {"vix": 33622528 + 2048, "viewshed": 34408448 + 367714816,
+                "site": 2495963392 + 11898112},
 }
 
 ROOFLINE_NOTES = {
