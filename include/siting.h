@@ -161,9 +161,12 @@ int siting_last_pick_order(siting_ctx *ctx, int32_t *order, int cap, int *count)
 
 /* Tracing: device clock cycles CTA 0 spent in each phase of the last SITE
  * run, summed over rounds: 0 set-up, 1 publishing its top keys, 2 round
- * barrier, 3 merging the lists and choosing the round's picks, 4 finding the
- * candidates near the picks, 5 compacting them, 6 gain deltas, 7 intervis cut
- * and second barrier, 8 applying the picks.  Writes min(n, 9) values. */
+ * barrier, 9 loading the published lists and keeping the exactly ordered
+ * keys, 10 ranking them, 3 choosing the round's picks, 4 finding the
+ * candidates near the picks (and, in large rounds, this CTA's rows of the
+ * picks' new bits), 11 the barrier after those rows (large rounds), 5
+ * compacting the pairs, 6 gain deltas, 12 intervis cut, 7 second barrier and
+ * the smallest cut, 8 applying the picks.  Writes min(n, 13) values. */
 int siting_last_site_phase_cycles(siting_ctx *ctx, long long *cycles, int n);
 
 /* SITE on device buffers without allocating any memory.  No counterpart in

@@ -376,8 +376,8 @@ class Context:
 
     def last_site_phase_cycles(self) -> list:
         """Device cycles per SITE phase (CTA 0) of the last run."""
-        out = (C.c_longlong * 9)()
-        self._check(self._lib.siting_last_site_phase_cycles(self.h, out, 9))
+        out = (C.c_longlong * 13)()
+        self._check(self._lib.siting_last_site_phase_cycles(self.h, out, 13))
         return list(out)
 
     # ---- whole pipeline ---------------------------------------------------------

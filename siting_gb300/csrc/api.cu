@@ -254,7 +254,7 @@ int site_enqueue(siting_ctx *ctx, int nrows, int roi, int intervis, int nsheds,
   CK(cudaMemsetAsync(d_selected, 0, nsheds, ctx->stream));
   CK(launch_site(nrows, roi, intervis, nsheds, d_obs, d_sheds, bs, nb, npb, d_selected, s, G,
                  d_err, ctx->stream));
-  CK(cudaMemcpyAsync(ctx->h_out, s.out, 12 * sizeof(long long), cudaMemcpyDeviceToHost,
+  CK(cudaMemcpyAsync(ctx->h_out, s.out, (3 + kSitePhases) * sizeof(long long), cudaMemcpyDeviceToHost,
                      ctx->stream));
   ctx->d_last_order = s.order;
   return SITING_OK;
@@ -602,7 +602,7 @@ int siting_last_pick_order(siting_ctx *ctx, int32_t *order, int cap, int *count)
 
 int siting_last_site_phase_cycles(siting_ctx *ctx, long long *cycles, int n) {
   if (!ctx || !cycles || n < 0) return SITING_EINVAL;
-  for (int i = 0; i < n && i < 9; i++) cycles[i] = ctx->h_out ? ctx->h_out[3 + i] : 0;
+  for (int i = 0; i < n && i < kSitePhases; i++) cycles[i] = ctx->h_out ? ctx->h_out[3 + i] : 0;
   return SITING_OK;
 }
 

@@ -78,11 +78,14 @@ struct SiteScratch {
   int *cuts;                 // [2][nctas]: per-CTA prefix cut (intervis)
   int *ncount;               // [2][64]: popcount of each pick's new bits (self-check)
   unsigned *bar;             // group barrier counter, zeroed
-  long long *out;            // [0] nused, [1] cumarea, [2] rounds, [3..9] phase cycles
+  long long *out;            // [0] nused, [1] cumarea, [2] rounds, [3..15] phase cycles
   int32_t *order;            // nsheds: picks in order
   int32_t *gains;            // nsheds: round-1 gains (site_score_kernel)
   void *table;               // job table of a one-job launch (site_job_table_bytes)
 };
+
+// Phases of the SITE tracing clocks (siting_last_site_phase_cycles).
+constexpr int kSitePhases = 13;
 
 // One SITE job (one DEM) of a launch.
 struct SiteJob {

@@ -195,7 +195,7 @@ __global__ void __launch_bounds__(kThreads, 1)
 
   GroupBarrier gb{a.bar, (unsigned)G, 0u};
   // tracing: device cycles per phase, accumulated by CTA 0's thread 0
-  long long ph[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+  long long ph[kSitePhases] = {};
   long long tmark = clock64();
   auto mark = [&](int i) {
     if (k == 0 && tid == 0) {
@@ -331,6 +331,7 @@ __global__ void __launch_bounds__(kThreads, 1)
       }
     }
     __syncthreads();
+    mark(9);
     const int nvalid = s_nvalid;
     {  // rank of each valid key: count larger valid keys, 32 at a time
       const int nch = (nvalid + 31) / 32;
@@ -352,6 +353,7 @@ __global__ void __launch_bounds__(kThreads, 1)
         s_near[s_vrank[v]] = 0;
       }
     __syncthreads();
+    mark(10);
     const int nrank = min(nvalid, kMaxPicks);
     // usable if > 2roi from every better-ranked entry: all pairs at once
     for (int i = tid; i < nrank * nrank; i += blockDim.x) {
@@ -593,6 +595,7 @@ __global__ void __launch_bounds__(kThreads, 1)
     } else {
     // every CTA's rows of N are written
     if (!group_sync(gb, a.err, &s_flagv)) return;
+    mark(11);
     if (nwpr <= 7) {
       // ---- D2. per (pair, row): popcount(placed(c) & N), loads issued together
       for (int it = tid; it < npair * nr; it += blockDim.x) {
@@ -736,6 +739,7 @@ __global__ void __launch_bounds__(kThreads, 1)
       __syncthreads();
       if (tid == 0) __stcg(a.cuts + par * G + k, s_roundcut);
     }
+    mark(12);
     // every read of the coverage this round is done once all CTAs pass here
     if (!group_sync(gb, a.err, &s_flagv)) return;
     if (tid == 0) s_mcut = m;
@@ -830,7 +834,7 @@ __global__ void __launch_bounds__(kThreads, 1)
     a.out[0] = npicks;
     a.out[1] = s_cum;
     a.out[2] = rounds;
-    for (int i = 0; i < 9; i++) a.out[3 + i] = ph[i];
+    for (int i = 0; i < kSitePhases; i++) a.out[3 + i] = ph[i];
   }
 }
 
