@@ -35,6 +35,39 @@ __device__ __forceinline__ int round_i(float v) {
   return __float2int_rz(__fadd_rn(v, h));
 }
 
+// Packed FP32 pairs (low half, high half) for the f32x2 instructions of
+// sm_100 and later: each half is an IEEE round-to-nearest operation of its
+// own, so a packed add or multiply equals two scalar ones bit for bit.
+__device__ __forceinline__ unsigned long long f2_pack(float lo, float hi) {
+  unsigned long long v;
+  asm("mov.b64 %0, {%1, %2};" : "=l"(v) : "f"(lo), "f"(hi));
+  return v;
+}
+__device__ __forceinline__ float f2_lo(unsigned long long v) {
+  float lo, hi;
+  asm("mov.b64 {%0, %1}, %2;" : "=f"(lo), "=f"(hi) : "l"(v));
+  return lo;
+}
+__device__ __forceinline__ float f2_hi(unsigned long long v) {
+  float lo, hi;
+  asm("mov.b64 {%0, %1}, %2;" : "=f"(lo), "=f"(hi) : "l"(v));
+  return hi;
+}
+__device__ __forceinline__ unsigned long long f2_add(unsigned long long a, unsigned long long b) {
+  unsigned long long d;
+  asm("add.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+  return d;
+}
+__device__ __forceinline__ unsigned long long f2_mul(unsigned long long a, unsigned long long b) {
+  unsigned long long d;
+  asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+  return d;
+}
+// copysign(pred(0.5), v): the addend of round_i for v's sign
+__device__ __forceinline__ float round_addend(float v) {
+  return __uint_as_float((__float_as_uint(v) & 0x80000000u) | 0x3effffffu);
+}
+
 // ---- memory-order helpers --------------------------------------------------
 __device__ __forceinline__ unsigned ld_acquire_u32(const unsigned *p) {
   unsigned v;

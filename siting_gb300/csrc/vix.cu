@@ -62,14 +62,17 @@ struct GlobalDem {
 // fall outside it and the bounds test is dropped.
 template <bool kInterior, class Dem>
 __device__ __forceinline__ int vix_target(const Dem &dem, int obase, int n, int roi, int roi2,
-                                          int tht, float span, int ox, int oy, int oz, float foz,
-                                          uint32_t r1, const float *rtab) {
+                                          int tht, unsigned long long span2, int ox, int oy,
+                                          int oz, float foz, uint32_t r1,
+                                          const unsigned long long *rtab2) {
   const uint32_t r2 = lcg_step(r1);
   // (int)((2*roi+0.99999f)*r/RANDOM_MAX): the divisor is 2^31, and scaling
   // by a power of two commutes with rounding (no overflow or underflow
-  // here), so RN(span*r)/2^31 = RN((span*2^-31)*r): span arrives pre-scaled.
-  int dx = f2i(fmul(span, i2f((int)r1))) - roi;
-  int dy = f2i(fmul(span, i2f((int)r2))) - roi;
+  // here), so RN(span*r)/2^31 = RN((span*2^-31)*r): span arrives pre-scaled,
+  // paired with itself, and both draws are scaled by one packed multiply.
+  const unsigned long long dd = f2_mul(span2, f2_pack(i2f((int)r1), i2f((int)r2)));
+  int dx = f2i(f2_lo(dd)) - roi;
+  int dy = f2i(f2_hi(dd)) - roi;
   if (dx * dx + dy * dy > roi2) {  // fold into the circle (siting.cpp:162-166)
     dx /= 3;
     dy /= 3;
@@ -83,22 +86,24 @@ __device__ __forceinline__ int vix_target(const Dem &dem, int obase, int n, int 
   const int tz = dem.at(obase + dx * W + dy) + tht;
   const bool mx = adx >= ady;
   const int d = mx ? dx : dy, m = mx ? dy : dx, ad = mx ? adx : ady;
-  const float rr = rtab[ad];  // |drecip| = (float)(1.0/|d|), siting.cpp:91
   // Sample offsets are id = +-1, 2, 4, ... along the major axis (the sign of
   // d).  slope*id = m*drecip*id = (m*|drecip|)*|id| exactly (negation and
   // scaling by a power of two are exact in FP32), likewise id*zslope, so both
   // are carried by doubling from m*|drecip| and (tz-oz)*|drecip|, bit-identical
-  // to the reference's products.  The sample's offset from the observer is
-  // id*(major stride) + round(slope*id)*(minor stride).
-  float sl = fmul(i2f(m), rr);
-  float zs = fmul(i2f(tz - oz), rr);
+  // to the reference's products.  They travel as one pair P = {slope*|id|,
+  // zslope*|id|}: one packed add doubles both, and one packed add with
+  // C = {copysign(pred(0.5), slope), oz} gives the rounding sum of the minor
+  // offset and the sight-line height oz + id*zslope.  The sample's offset
+  // from the observer is id*(major stride) + round(slope*id)*(minor stride).
+  unsigned long long P = f2_mul(f2_pack(i2f(m), i2f(tz - oz)), rtab2[ad]);  // |drecip|, siting.cpp:91
+  const unsigned long long C = f2_pack(round_addend(f2_lo(P)), foz);  // the sign never changes
   const int smin = mx ? 1 : W;
   int q = obase + (mx ? (d > 0 ? W : -W) : (d > 0 ? 1 : -1));  // observer + id*(major stride)
   for (int step = 1; step < ad; step <<= 1) {
-    const int off = round_i(sl);
-    if (i2f(dem.at(q + off * smin)) > fadd(foz, zs)) return 0;
-    sl = fadd(sl, sl);
-    zs = fadd(zs, zs);
+    const unsigned long long Q = f2_add(P, C);
+    const int off = f2i(f2_lo(Q));  // round(slope*id), half away from zero
+    if (i2f(dem.at(q + off * smin)) > f2_hi(Q)) return 0;
+    P = f2_add(P, P);
     q = 2 * q - obase;  // id doubles
   }
   return 1;
@@ -111,11 +116,12 @@ __device__ __forceinline__ int vix_target(const Dem &dem, int obase, int n, int 
 template <bool kInterior, class Dem>
 __device__ __forceinline__ void vix_tile_work(const Dem &dem, const VixArgs &a,
                                               const int4 *cinfo, const uint2 *jump,
-                                              const float *rtab, int *cnt) {
+                                              const unsigned long long *rtab2, int *cnt) {
   const int ncell = a.tile * a.tile;
   const int L = max(1, (int)blockDim.x / ncell);  // a power of two: tiles are 16, 32, 64
   const int per_pass = blockDim.x / L;
   const float span = fmul(fadd(i2f(2 * a.roi), 0.99999f), 0x1p-31f);  // scaled by 2^-31
+  const unsigned long long span2 = f2_pack(span, span);
   const int roi2 = a.roi * a.roi;
   const int sub = threadIdx.x & (L - 1);
   for (int c0 = 0; c0 < ncell; c0 += per_pass) {
@@ -130,8 +136,8 @@ __device__ __forceinline__ void vix_tile_work(const Dem &dem, const VixArgs &a,
         for (int t = sub; t < a.ntests; t += L) {
           const uint2 j = jump[t];
           const uint32_t r1 = (j.x * seed + j.y) & 0x7fffffffu;
-          acc += vix_target<kInterior>(dem, obase, a.n, a.roi, roi2, a.tht, span, ox, oy, oz, foz,
-                                       r1, rtab);
+          acc += vix_target<kInterior>(dem, obase, a.n, a.roi, roi2, a.tht, span2, ox, oy, oz,
+                                       foz, r1, rtab2);
         }
       }
     }
@@ -157,8 +163,8 @@ __global__ void __launch_bounds__(1024) vix_kernel(const __grid_constant__ CUten
   off += 16;
   uint2 *jump = reinterpret_cast<uint2 *>(sm + off);
   off += (size_t)a.ntests * 8;
-  float *rtab = reinterpret_cast<float *>(sm + off);
-  off += (size_t)(a.roi + 1) * 4;
+  unsigned long long *rtab2 = reinterpret_cast<unsigned long long *>(sm + off);  // {r, r} pairs
+  off += (size_t)(a.roi + 1) * 8;
   int *cnt = reinterpret_cast<int *>(sm + off);
   off += (size_t)T * T * 4;
   off = (off + 15) & ~(size_t)15;
@@ -175,7 +181,7 @@ __global__ void __launch_bounds__(1024) vix_kernel(const __grid_constant__ CUten
   }
   for (int i = threadIdx.x; i < a.ntests; i += blockDim.x)
     jump[i] = make_uint2(a.jump[2 * i], a.jump[2 * i + 1]);
-  for (int i = threadIdx.x; i <= a.roi; i += blockDim.x) rtab[i] = a.rtab[i];
+  for (int i = threadIdx.x; i <= a.roi; i += blockDim.x) rtab2[i] = f2_pack(a.rtab[i], a.rtab[i]);
   for (int i = threadIdx.x; i <= a.ntests; i += blockDim.x) vtab[i] = a.vtab[i];
   __syncthreads();
 
@@ -205,16 +211,16 @@ __global__ void __launch_bounds__(1024) vix_kernel(const __grid_constant__ CUten
     const SmemDem dem{halo, a.halo_w, hx0, hy0};
     fill_cells(dem);
     if (interior)
-      vix_tile_work<true>(dem, a, cinfo, jump, rtab, cnt);
+      vix_tile_work<true>(dem, a, cinfo, jump, rtab2, cnt);
     else
-      vix_tile_work<false>(dem, a, cinfo, jump, rtab, cnt);
+      vix_tile_work<false>(dem, a, cinfo, jump, rtab2, cnt);
   } else {
     const GlobalDem dem{a.dem, a.pitch};
     fill_cells(dem);
     if (interior)
-      vix_tile_work<true>(dem, a, cinfo, jump, rtab, cnt);
+      vix_tile_work<true>(dem, a, cinfo, jump, rtab2, cnt);
     else
-      vix_tile_work<false>(dem, a, cinfo, jump, rtab, cnt);
+      vix_tile_work<false>(dem, a, cinfo, jump, rtab2, cnt);
   }
   __syncthreads();
   for (int i = threadIdx.x; i < T * T; i += blockDim.x) {
@@ -240,9 +246,9 @@ HaloGeom halo_geom(int tile, int roi) {
 }
 
 size_t tables_tail_bytes(int tile, int roi, int ntests) {
-  // mbarrier, jump table, reciprocals, counts, then the int4 cell table
+  // mbarrier, jump table, reciprocal pairs, counts, then the int4 cell table
   // (16-byte aligned: the offsets before it are multiples of 4), VIX bytes
-  size_t b = 16 + (size_t)ntests * 8 + (size_t)(roi + 1) * 4 + (size_t)tile * tile * 4;
+  size_t b = 16 + (size_t)ntests * 8 + (size_t)(roi + 1) * 8 + (size_t)tile * tile * 4;
   b = (b + 15) & ~(size_t)15;
   return b + (size_t)tile * tile * 16 + ntests + 1;
 }
