@@ -426,16 +426,36 @@ __global__ void __launch_bounds__(kThreads, 1)
         int fwp, fbp;
         shed_align(py - roi, fwp, fbp);
         const int gr = px - roi + prow;
+        const bool row_in = gr >= 0 && gr < n;
         uint64_t *nrow = a.nbits + (size_t)(pi * nr + prow) * nb2;
         const uint64_t *prw = a.sheds + (size_t)s_pk[pi] * per + (size_t)prow * nwpr;
         int cnt = 0;
-        for (int j = 0; j < nb2; j++) {
-          const int W = fwp + j;
-          uint64_t v = 0ull;
-          if (gr >= 0 && gr < n && W >= 0 && W < cw)
-            v = placed_word(prw, j, nwpr, fbp) & ~__ldcg(cum + (size_t)gr * cw + W);
-          __stcg(nrow + j, v);
-          cnt += __popcll(v);
+        if (nwpr <= 7) {  // all of the row's loads issued together
+          const uint64_t *xr = cum + (size_t)(row_in ? gr : 0) * cw;
+          uint64_t w[8], x[8];
+#pragma unroll
+          for (int q = 0; q < 8; q++) {
+            w[q] = q < nwpr ? __ldg(prw + q) : 0ull;
+            const int W = fwp + q;
+            x[q] = (row_in && q < nb2 && W >= 0 && W < cw) ? __ldcg(xr + W) : ~0ull;
+          }
+#pragma unroll
+          for (int q = 0; q < 8; q++) {
+            if (q >= nb2) break;
+            const uint64_t v =
+                ((w[q] >> fbp) | ((q > 0 && fbp) ? w[q - 1] << (64 - fbp) : 0ull)) & ~x[q];
+            __stcg(nrow + q, v);
+            cnt += __popcll(v);
+          }
+        } else {
+          for (int j = 0; j < nb2; j++) {
+            const int W = fwp + j;
+            uint64_t v = 0ull;
+            if (row_in && W >= 0 && W < cw)
+              v = placed_word(prw, j, nwpr, fbp) & ~__ldcg(cum + (size_t)gr * cw + W);
+            __stcg(nrow + j, v);
+            cnt += __popcll(v);
+          }
         }
         if (cnt) atomicAdd(a.ncount + par * kMaxPicks + pi, cnt);
       }
@@ -596,7 +616,63 @@ __global__ void __launch_bounds__(kThreads, 1)
     // every CTA's rows of N are written
     if (!group_sync(gb, a.err, &s_flagv)) return;
     mark(11);
-    if (nwpr <= 7) {
+    if (kThreads == 512 && nwpr <= 4) {
+      // ---- D2 for narrow sheds: two (pair, row) items a thread in flight
+      // (512-thread CTAs only: the 1024-thread build has no registers for it).
+      // An item's loads: c's row (w) and the pick's new bits under it (x);
+      // pr < 0 marks an item with nothing to count.
+      auto load_item = [&](int it, uint64_t(&w)[4], uint64_t(&x)[5], int &pr, int &fbc) {
+        pr = -1;
+        if (it >= npair * nr) return;
+        const int u = it / nr, r = it - u * nr;
+        const int pq = s_plist[u];
+        const int pi = pq / pcap;
+        const int s = s_pairslot[pq];
+        const int cp = s_pos[s], pp = s_ppos[pi];
+        const int cx = cp >> 16, cy = cp & 0xffff, px = pp >> 16, py = pp & 0xffff;
+        const int gr = cx - roi + r, prow = gr - (px - roi);
+        if (prow < 0 || prow >= nr || gr < 0 || gr >= n) return;
+        int fwc, fwp, fbp;
+        shed_align(cy - roi, fwc, fbc);
+        shed_align(py - roi, fwp, fbp);
+        const uint64_t *nrow = a.nbits + (size_t)(pi * nr + prow) * nb2;
+        if (a.intervis && r == roi) {  // own cell: newly covered by the pick?
+          const int j = (cy >> 6) - fwp;
+          if (j >= 0 && j < nb2 && ((__ldcg(nrow + j) >> (63 - (cy & 63))) & 1ull))
+            atomicOr(reinterpret_cast<unsigned *>(s_paircov + (pq & ~3)), 1u << (8 * (pq & 3)));
+        }
+        const int lo = max(max(fwc, fwp), 0);
+        const int hi = min(min((cy + roi) >> 6, fwp + nwpr), cw - 1);
+        if (lo > hi) return;
+        const uint64_t *crow = a.sheds + (size_t)(s * G + k) * per + (size_t)r * nwpr;
+#pragma unroll
+        for (int q = 0; q < 4; q++) w[q] = q < nwpr ? __ldg(crow + q) : 0ull;
+#pragma unroll
+        for (int q = 0; q < 5; q++) {
+          const int W = fwc + q;  // c's placed word q lands at column word fwc+q
+          x[q] = (q < nb2 && W >= lo && W <= hi) ? __ldcg(nrow + (W - fwp)) : 0ull;
+        }
+        pr = pq;
+      };
+      auto count_item = [&](const uint64_t(&w)[4], const uint64_t(&x)[5], int pr, int fbc) {
+        int d = 0;
+#pragma unroll
+        for (int q = 0; q < 5; q++) {
+          const uint64_t cur = q < 4 ? w[q] : 0ull;
+          const uint64_t vc = (cur >> fbc) | ((q > 0 && fbc) ? w[q - 1] << (64 - fbc) : 0ull);
+          d += __popcll(vc & x[q]);
+        }
+        if (d) atomicAdd(&s_pairdelta[pr], d);
+      };
+      for (int it = tid; it < npair * nr; it += 2 * blockDim.x) {
+        uint64_t w0[4], x0[5], w1[4], x1[5];
+        int pr0, pr1, fb0 = 0, fb1 = 0;
+        load_item(it, w0, x0, pr0, fb0);
+        load_item(it + blockDim.x, w1, x1, pr1, fb1);
+        if (pr0 >= 0) count_item(w0, x0, pr0, fb0);
+        if (pr1 >= 0) count_item(w1, x1, pr1, fb1);
+      }
+    } else if (nwpr <= 7) {
       // ---- D2. per (pair, row): popcount(placed(c) & N), loads issued together
       for (int it = tid; it < npair * nr; it += blockDim.x) {
         const int u = it / nr, r = it - u * nr;

@@ -154,9 +154,11 @@ __device__ __forceinline__ void sweep_rays(const Dem &dem, const ShedArgs &a, in
       const int off = round_i(fmul(fai, sl));
       const float fe = i2f(dem.at(pb + off * smin));
       const float fa = __fsub_rn(fe, foalt);
-      // s = RN(a/|i|) can exceed hs only if a > hs*|i|; the sign of the fused
-      // hs*|i| - a is exact, so the division runs only when the horizon may rise
-      if (__fmaf_rn(hs, fai, -fa) < 0.f) {
+      // s = RN(a/|i|) can exceed hs only if a > hs*|i|, and then t = RN(hs*|i|)
+      // <= a (rounding is monotone and a is a float): the division runs only
+      // when the horizon may rise, and t serves the visibility test as well
+      float t = fmul(hs, fai);
+      if (t <= fa) {
         float s;
         if (kRcp) {
           const float y = rcp[__float2int_rz(fai)];
@@ -165,9 +167,12 @@ __device__ __forceinline__ void sweep_rays(const Dem &dem, const ShedArgs &a, in
         } else {
           s = fdiv(fa, fai);
         }
-        if (hs < s) hs = s;
+        if (hs < s) {
+          hs = s;
+          t = fmul(hs, fai);
+        }
       }
-      if (fadd(fe, ftht) >= fadd(foalt, fmul(hs, fai)))
+      if (fadd(fe, ftht) >= fadd(foalt, t))
         atomicOr(&img[(off + roi) * stride + (pos >> 5)], 1u << (pos & 31));
     }
   }
