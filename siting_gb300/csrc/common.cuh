@@ -44,13 +44,13 @@ __device__ __forceinline__ unsigned long long f2_pack(float lo, float hi) {
   return v;
 }
 __device__ __forceinline__ float f2_lo(unsigned long long v) {
-  float lo, hi;
-  asm("mov.b64 {%0, %1}, %2;" : "=f"(lo), "=f"(hi) : "l"(v));
+  float lo;
+  asm("{\n\t.reg .f32 t;\n\tmov.b64 {%0, t}, %1;\n\t}" : "=f"(lo) : "l"(v));
   return lo;
 }
 __device__ __forceinline__ float f2_hi(unsigned long long v) {
-  float lo, hi;
-  asm("mov.b64 {%0, %1}, %2;" : "=f"(lo), "=f"(hi) : "l"(v));
+  float hi;
+  asm("{\n\t.reg .f32 t;\n\tmov.b64 {t, %0}, %1;\n\t}" : "=f"(hi) : "l"(v));
   return hi;
 }
 __device__ __forceinline__ unsigned long long f2_add(unsigned long long a, unsigned long long b) {

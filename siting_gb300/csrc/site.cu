@@ -104,6 +104,14 @@ __device__ __forceinline__ unsigned long long make_key(int area, int c) {
 __device__ __forceinline__ int key_index(unsigned long long key) {
   return (int)(0xFFFFFFFFu - (unsigned)(key & 0xFFFFFFFFull));
 }
+// Largest 64-bit key of a full warp by two 32-bit reductions: the largest
+// high word, then the largest low word among the lanes that hold it.
+__device__ __forceinline__ unsigned long long warp_max_key(unsigned long long key) {
+  const unsigned hi = (unsigned)(key >> 32), lo = (unsigned)key;
+  const unsigned mh = __reduce_max_sync(0xffffffffu, hi);
+  const unsigned ml = __reduce_max_sync(0xffffffffu, hi == mh ? lo : 0u);
+  return ((unsigned long long)mh << 32) | ml;
+}
 
 // Slot flags
 constexpr unsigned char kUsed = 1, kInel = 4;
@@ -240,12 +248,7 @@ __global__ void __launch_bounds__(kThreads, 1)
       unsigned long long key = 0;
       if (s < my_slots && !(s_flag[s] & kUsed)) key = make_key(s_area[s], s * G + k);
       for (int e = 0; e < kTopK; e++) {
-        unsigned long long mx = key;
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) {
-          const unsigned long long w = __shfl_xor_sync(0xffffffffu, mx, o);
-          mx = w > mx ? w : mx;
-        }
+        const unsigned long long mx = warp_max_key(key);
         if (lane == 0) s_gtop[g * kTopK + e] = mx;
         if (key == mx) key = 0;  // keys are unique (the index is part of them)
       }
@@ -270,16 +273,10 @@ __global__ void __launch_bounds__(kThreads, 1)
             }
           }
         }
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) {
-          const unsigned long long w = __shfl_xor_sync(0xffffffffu, key, o);
-          const int wg = __shfl_xor_sync(0xffffffffu, gi, o);
-          if (w > key) {
-            key = w;
-            gi = wg;
-          }
-        }
-        if (key && lane == (gi & 31)) {
+        // keys are unique: the lane holding the largest advances that head
+        const unsigned long long mine = key;
+        key = warp_max_key(mine);
+        if (key && mine == key) {
           const int q = gi >> 5;
           h0 += q == 0;
           h1 += q == 1;
@@ -309,11 +306,7 @@ __global__ void __launch_bounds__(kThreads, 1)
     {  // exactness threshold: unpublished keys are below each full list's last key
       unsigned long long T = 0;
       if (tid < G) T = s_mkey[tid * kTopK + kTopK - 1];
-#pragma unroll
-      for (int o = 16; o > 0; o >>= 1) {
-        const unsigned long long w = __shfl_xor_sync(0xffffffffu, T, o);
-        T = w > T ? w : T;
-      }
+      T = warp_max_key(T);
       if (lane == 0 && warp * 32 < G) s_red[warp] = T;
     }
     __syncthreads();
@@ -321,6 +314,9 @@ __global__ void __launch_bounds__(kThreads, 1)
       unsigned long long T = 0;
       for (int w = 0; w * 32 < G; w++) T = s_red[w] > T ? s_red[w] : T;
       // exactly ordered entries: keys >= T with a positive area
+      auto valid_key = [&](unsigned long long key) {
+        return key != 0 && (key >> 32) != 0 && key >= T;
+      };
       for (int e = tid; e < GK; e += blockDim.x) {
         const unsigned long long key = s_mkey[e];
         if (key == 0 || (key >> 32) == 0 || key < T) continue;
@@ -619,6 +615,7 @@ __global__ void __launch_bounds__(kThreads, 1)
     if (kThreads == 512 && nwpr <= 4) {
       // ---- D2 for narrow sheds: two (pair, row) items a thread in flight
       // (512-thread CTAs only: the 1024-thread build has no registers for it).
+      // Items past the end load nothing (pr < 0).
       // An item's loads: c's row (w) and the pick's new bits under it (x);
       // pr < 0 marks an item with nothing to count.
       auto load_item = [&](int it, uint64_t(&w)[4], uint64_t(&x)[5], int &pr, int &fbc) {
