@@ -172,7 +172,9 @@ __device__ __forceinline__ void sweep_rays(const Dem &dem, const ShedArgs &a, in
           t = fmul(hs, fai);
         }
       }
-      if (fadd(fe, ftht) >= fadd(foalt, t))
+      // pelev + tht against oalt + hs*|i|: both sums in one packed add
+      const unsigned long long V = f2_add(f2_pack(fe, foalt), f2_pack(ftht, t));
+      if (f2_lo(V) >= f2_hi(V))
         atomicOr(&img[(off + roi) * stride + (pos >> 5)], 1u << (pos & 31));
     }
   }
