@@ -157,7 +157,6 @@ __global__ void __launch_bounds__(kThreads, 1)
   __shared__ int s_poff[kMaxPicks + 1];
   __shared__ unsigned long long s_red[32];
   __shared__ int s_rank[kMaxPicks], s_rpos[kMaxPicks];
-  __shared__ unsigned char s_near[kMaxPicks];
 
   const int G = a.G, k = blockIdx.x - a.block0;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nwarps = blockDim.x >> 5;
@@ -317,22 +316,32 @@ __global__ void __launch_bounds__(kThreads, 1)
       auto valid_key = [&](unsigned long long key) {
         return key != 0 && (key >> 32) != 0 && key >= T;
       };
-      for (int e = tid; e < GK; e += blockDim.x) {
-        const unsigned long long key = s_mkey[e];
-        if (key == 0 || (key >> 32) == 0 || key < T) continue;
-        const int v = atomicAdd(&s_nvalid, 1);
-        s_valid[v] = e;  // GK entries fit
-        s_vkey[v] = key;
-        s_vrank[v] = 0;
+      for (int e0 = warp * 32; e0 < GK; e0 += blockDim.x) {  // one shared atomic a warp
+        const int e = e0 + lane;
+        const unsigned long long key = e < GK ? s_mkey[e] : 0ull;
+        const bool ok = key != 0 && (key >> 32) != 0 && key >= T;
+        const unsigned bal = __ballot_sync(0xffffffffu, ok);
+        if (!bal) continue;
+        int v0 = 0;
+        if (lane == 0) v0 = atomicAdd(&s_nvalid, __popc(bal));
+        v0 = __shfl_sync(0xffffffffu, v0, 0);
+        if (ok) {
+          const int v = v0 + __popc(bal & ((1u << lane) - 1u));
+          s_valid[v] = e;  // GK entries fit
+          s_vkey[v] = key;
+          s_vrank[v] = 0;
+        }
       }
     }
     __syncthreads();
     mark(9);
     const int nvalid = s_nvalid;
     {  // rank of each valid key: count larger valid keys, 32 at a time
+      // lanes take consecutive keys against one chunk: the chunk's reads are
+      // broadcasts, free of bank conflicts
       const int nch = (nvalid + 31) / 32;
       for (int i = tid; i < nvalid * nch; i += blockDim.x) {
-        const int v = i / nch, c0 = (i - v * nch) * 32;
+        const int ch = i / nvalid, v = i - ch * nvalid, c0 = ch * 32;
         const unsigned long long key = s_vkey[v];
         const int c1 = min(c0 + 32, nvalid);
         int cnt = 0;
@@ -346,44 +355,36 @@ __global__ void __launch_bounds__(kThreads, 1)
       if (s_vrank[v] < kMaxPicks) {
         s_rank[s_vrank[v]] = s_valid[v];
         s_rpos[s_vrank[v]] = s_mpos[s_valid[v]];
-        s_near[s_vrank[v]] = 0;
       }
     __syncthreads();
     mark(10);
     const int nrank = min(nvalid, kMaxPicks);
-    // usable if > 2roi from every better-ranked entry: all pairs at once
-    for (int i = tid; i < nrank * nrank; i += blockDim.x) {
-      const int r1 = i / nrank, r0 = i - r1 * nrank;
-      if (r0 >= r1) continue;
-      const int p1 = s_rpos[r1], p0 = s_rpos[r0];
-      const int dx = (p1 >> 16) - (p0 >> 16), dy = (p1 & 0xffff) - (p0 & 0xffff);
-      if (dx * dx + dy * dy <= lim2) s_near[r1] = 1;
-    }
-    __syncthreads();
-    if (warp == 0) {  // prefix: leading usable ranks, capped, up to the 95% stop
+    if (warp == 0) {
+      // prefix: leading ranks that are each > 2roi from every better-ranked
+      // one, capped, up to the 95% stop.  Lane l holds ranks l and l+32.
       const int max_m = min(kMaxPicks, a.pair_cap / max(pcap, 1));
+      const int lim = min(nrank, max_m);
+      const int q0 = lane < lim ? s_rpos[lane] : 0;
+      const int q1 = lane + 32 < lim ? s_rpos[lane + 32] : 0;
+      const int a0 = lane < lim ? (int)(s_mkey[s_rank[lane]] >> 32) : 0;
+      const int a1 = lane + 32 < lim ? (int)(s_mkey[s_rank[lane + 32]] >> 32) : 0;
       long long cumv = s_cum;
       int m = 0, stop_at = -1;
-      for (int base = 0; base < nrank && base < max_m; base += 32) {
-        const int r = base + lane;
-        const bool ok = r < nrank && r < max_m && !s_near[r];
-        const unsigned okm = __ballot_sync(0xffffffffu, ok);
-        const int run = okm == 0xffffffffu ? 32 : __ffs(~okm) - 1;
-        long long v = lane < run ? (long long)(s_mkey[s_rank[r]] >> 32) : 0;
-#pragma unroll
-        for (int o = 1; o < 32; o <<= 1) {
-          const long long w = __shfl_up_sync(0xffffffffu, v, o);
-          if (lane >= o) v += w;
-        }
-        const unsigned hit = __ballot_sync(0xffffffffu, lane < run && cumv + v >= a.stop_area);
-        if (hit) {
-          m = base + __ffs(hit);
+      for (int r = 0; r < lim; r++) {
+        const int p1 = __shfl_sync(0xffffffffu, r < 32 ? q0 : q1, r & 31);
+        const int area = __shfl_sync(0xffffffffu, r < 32 ? a0 : a1, r & 31);
+        const int x1 = p1 >> 16, y1 = p1 & 0xffff;
+        const int dx0 = (q0 >> 16) - x1, dy0 = (q0 & 0xffff) - y1;
+        const int dx1 = (q1 >> 16) - x1, dy1 = (q1 & 0xffff) - y1;
+        const bool near = (lane < r && dx0 * dx0 + dy0 * dy0 <= lim2) ||
+                          (lane + 32 < r && dx1 * dx1 + dy1 * dy1 <= lim2);
+        if (__any_sync(0xffffffffu, near)) break;
+        cumv += area;
+        m = r + 1;
+        if (cumv >= a.stop_area) {
           stop_at = m;
           break;
         }
-        m = base + run;
-        cumv += __shfl_sync(0xffffffffu, v, 31);
-        if (run < 32) break;
       }
       for (int j = lane; j < m; j += 32) {
         const int e = s_rank[j];
