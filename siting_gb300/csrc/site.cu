@@ -416,7 +416,9 @@ __global__ void __launch_bounds__(kThreads, 1)
     // self-check
     if (dist) {
       const int rows_mine = k < nr ? (nr - k + G - 1) / G : 0;
-      for (int i = tid; i < m * rows_mine; i += blockDim.x) {
+      // taken from the last thread down, so that these rows overlap the
+      // neighbour search below, whose items start at thread 0
+      for (int i = blockDim.x - 1 - tid; i < m * rows_mine; i += blockDim.x) {
         const int pi = i / rows_mine, prow = k + G * (i - (i / rows_mine) * rows_mine);
         const int pp = s_ppos[pi];
         const int px = pp >> 16, py = pp & 0xffff;
