@@ -300,17 +300,16 @@ def stage_bytes(w, nwanted, site_bytes):
 
 
 # DRAM bytes per launch (dram__bytes_read.sum + dram__bytes_write.sum) from
-# ncu: SITE and VIEWSHED captured at full size (profiles/launches_c2_4096.md),
-# VIX from the 2048^2 capture of the same parameters scaled by cells
-# (profiles/vix_kernel_c2_2048.md; its traffic is the DEM read once).
+# ncu: VIX, VIEWSHED and SITE captured at full size (profiles/launches_c2_4096.md).
 NCU_TRAFFIC = {
-    "c2_4096": {"vix": 33622528 + 2048, "viewshed": 34408448 + 367714816,
-                "site": 2495963392 + 11898112},
+    "c2_4096": {"vix": 33571072 + 6400, "viewshed": 34218496 + 362720768,
+                "site": 2496145152 + 11676672},
 }
 
 ROOFLINE_NOTES = {
     "vix": "VIX is SM-issue bound, not HBM bound: its compulsory traffic is 3 B/cell and ncu shows "
-           "93.0% issue-active cycles (profiles/vix_kernel_c2_2048.md)",
+           "89.8% issue-active cycles, 3.57 warp instructions a cycle of 4 "
+           "(profiles/vix_kernel_c2_2048.md)",
     "site": "SITE's algorithmic bytes are the reference's rescoring traffic (every rescored "
             "candidate's shed and coverage window per pick); this kernel updates gains by "
             "per-pick deltas and reads less (traffic), and is bound by the latency of its "
