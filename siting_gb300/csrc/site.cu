@@ -104,6 +104,16 @@ __device__ __forceinline__ unsigned long long make_key(int area, int c) {
 __device__ __forceinline__ int key_index(unsigned long long key) {
   return (int)(0xFFFFFFFFu - (unsigned)(key & 0xFFFFFFFFull));
 }
+// Division by an invariant divisor d >= 1: r = ceil(2^64/d) (0 for d = 1)
+// gives floor(n/d) = high 64 bits of n*r for every n < 2^32, since n*r/2^64
+// exceeds n/d by less than n/2^64 < 1/d (Granlund and Montgomery, 1994).
+__host__ __device__ __forceinline__ unsigned long long div_recip(int d) {
+  return d > 1 ? ~0ull / (unsigned long long)d + 1ull : 0ull;
+}
+__device__ __forceinline__ int div_by(int n, unsigned long long r) {
+  return r ? (int)__umul64hi((unsigned long long)(unsigned)n, r) : n;
+}
+
 // Largest 64-bit key of a full warp by two 32-bit reductions: the largest
 // high word, then the largest low word among the lanes that hold it.
 __device__ __forceinline__ unsigned long long warp_max_key(unsigned long long key) {
@@ -155,6 +165,10 @@ __global__ void __launch_bounds__(kThreads, 1)
   __shared__ int s_m, s_mcut, s_stop_at, s_done, s_flagv, s_roundcut, s_npair, s_nvalid;
   __shared__ long long s_cum;
   __shared__ int s_poff[kMaxPicks + 1];
+  // reciprocals (div_recip) of the kernel's divisors and of each pick's run
+  __shared__ unsigned long long s_rG, s_rnr, s_rpcap, s_rm, s_rrows, s_rnb2;
+  __shared__ unsigned long long s_rrun[kMaxPicks];
+  __shared__ int4 s_pbox[kMaxPicks];  // per pick: start of its first block row, run, per_run, items
   __shared__ unsigned long long s_red[32];
   __shared__ int s_rank[kMaxPicks], s_rpos[kMaxPicks];
 
@@ -169,6 +183,14 @@ __global__ void __launch_bounds__(kThreads, 1)
   const int ngroups = (a.nslots + 31) / 32;
   const int GK = G * kTopK;
   const int pcap = a.pick_cap;
+  const int rows_mine = k < nr ? (nr - k + G - 1) / G : 0;  // coverage rows this CTA owns
+  if (tid == 0) {
+    s_rG = div_recip(G);
+    s_rnr = div_recip(nr);
+    s_rpcap = div_recip(pcap);
+    s_rrows = div_recip(max(rows_mine, 1));
+    s_rnb2 = div_recip(nb2);
+  }
 
   // shared-memory carve-up (sizes mirrored by site_smem_bytes)
   unsigned char *p = sm;
@@ -201,14 +223,18 @@ __global__ void __launch_bounds__(kThreads, 1)
   uint64_t *s_N = reinterpret_cast<uint64_t *>(take((size_t)a.ncap_words * 8));
 
   GroupBarrier gb{a.bar, (unsigned)G, 0u};
-  // tracing: device cycles per phase, accumulated by CTA 0's thread 0
-  long long ph[kSitePhases] = {};
-  long long tmark = clock64();
+  // tracing: device cycles per phase, accumulated by CTA 0's thread 0 in
+  // shared memory (a register array would take registers in every thread)
+  __shared__ long long s_ph[kSitePhases], s_tmark;
+  if (tid == 0) {
+    for (int i = 0; i < kSitePhases; i++) s_ph[i] = 0;
+    s_tmark = clock64();
+  }
   auto mark = [&](int i) {
     if (k == 0 && tid == 0) {
       const long long now = clock64();
-      ph[i] += now - tmark;
-      tmark = now;
+      s_ph[i] += now - s_tmark;
+      s_tmark = now;
     }
   };
 
@@ -393,10 +419,24 @@ __global__ void __launch_bounds__(kThreads, 1)
         s_ppos[j] = s_mpos[e];
         s_pkey[j] = s_mkey[e];
         prefetch_l2(a.sheds + (size_t)c * per, per * 8);  // the pick's shed, for D1
+        {  // the block rectangle of the neighbour search (FINDMAX geometry, +-2 blocks)
+          const float r2f = (float)(2 * roi);
+          const int pos = s_mpos[e];
+          const int px = pos >> 16, py = pos & 0xffff;
+          const int bxl = max(0, (int)floorf(((float)px - r2f) / a.bs) - 2);
+          const int bxh = min(a.nb - 1, (int)floorf(((float)px + r2f) / a.bs) + 2);
+          const int byl = max(0, (int)floorf(((float)py - r2f) / a.bs) - 2);
+          const int byh = min(a.nb - 1, (int)floorf(((float)py + r2f) / a.bs) + 2);
+          const int run = (byh - byl + 1) * a.npb;
+          const int per_run = run / G + 2;
+          s_pbox[j] = make_int4((bxl * a.nb + byl) * a.npb, run, per_run, (bxh - bxl + 1) * per_run);
+          s_rrun[j] = div_recip(per_run);
+        }
       }
       if (lane == 0) {
         s_m = m;
         s_stop_at = stop_at;
+        s_rm = div_recip(max(m, 1));
       }
     }
     __syncthreads();
@@ -415,11 +455,11 @@ __global__ void __launch_bounds__(kThreads, 1)
     // ---- D1 (spread): this CTA's rows of every pick, popcounts for the
     // self-check
     if (dist) {
-      const int rows_mine = k < nr ? (nr - k + G - 1) / G : 0;
+      const unsigned long long rr = s_rrows;
       // taken from the last thread down, so that these rows overlap the
       // neighbour search below, whose items start at thread 0
       for (int i = blockDim.x - 1 - tid; i < m * rows_mine; i += blockDim.x) {
-        const int pi = i / rows_mine, prow = k + G * (i - (i / rows_mine) * rows_mine);
+        const int pi = div_by(i, rr), prow = k + G * (i - pi * rows_mine);
         const int pp = s_ppos[pi];
         const int px = pp >> 16, py = pp & 0xffff;
         int fwp, fbp;
@@ -462,23 +502,20 @@ __global__ void __launch_bounds__(kThreads, 1)
 
     // ---- C. own unused candidates within 2*roi of each pick ------------------
     {
-      const float r2f = (float)(2 * roi);
+      const unsigned long long rm = s_rm, rG = s_rG;
       for (int i = tid; i < m * a.pick_items; i += blockDim.x) {
-        const int pi = i % m, it = i / m;
+        const int it = div_by(i, rm), pi = i - it * m;
+        const int4 box = s_pbox[pi];  // first start, run, per_run, items
+        if (it >= box.w) continue;
         const int pos = s_ppos[pi];
         const int px = pos >> 16, py = pos & 0xffff;
-        const int bxl = max(0, (int)floorf(((float)px - r2f) / a.bs) - 2);
-        const int bxh = min(a.nb - 1, (int)floorf(((float)px + r2f) / a.bs) + 2);
-        const int byl = max(0, (int)floorf(((float)py - r2f) / a.bs) - 2);
-        const int byh = min(a.nb - 1, (int)floorf(((float)py + r2f) / a.bs) + 2);
-        const int run = (byh - byl + 1) * a.npb;
-        const int per_run = run / G + 2;
-        if (it >= (bxh - bxl + 1) * per_run) continue;
-        const int r = it / per_run, mm = it - r * per_run;
-        const int start = ((bxl + r) * a.nb + byl) * a.npb;
-        const int c = start + ((k - start % G) + G) % G + mm * G;
-        if (c >= start + run || c >= a.nsheds || c == s_pk[pi]) continue;
-        const int s = c / G;
+        const int r = div_by(it, s_rrun[pi]), mm = it - r * box.z;
+        const int start = box.x + r * a.nb * a.npb;
+        int off = k - (start - div_by(start, rG) * G);  // first index owned by this CTA
+        if (off < 0) off += G;
+        const int c = start + off + mm * G;
+        if (c >= start + box.y || c >= a.nsheds || c == s_pk[pi]) continue;
+        const int s = div_by(c, rG);
         if (s_flag[s] & kUsed) continue;
         const int cp = s_pos[s];
         const int cx = cp >> 16, cy = cp & 0xffff;
@@ -529,7 +566,7 @@ __global__ void __launch_bounds__(kThreads, 1)
     }
     __syncthreads();
     for (int i = tid; i < m * pcap; i += blockDim.x) {
-      const int j = i / pcap, q = i - j * pcap;
+      const int j = div_by(i, s_rpcap), q = i - j * pcap;
       if (q < min(s_pcnt[j], pcap)) s_plist[s_poff[j] + q] = i;
     }
     __syncthreads();
@@ -576,9 +613,9 @@ __global__ void __launch_bounds__(kThreads, 1)
       __syncthreads();
       // ---- D2. per (pair, row): popcount(placed(c) & N) ----------------------
       for (int it = tid; it < npair * nr; it += blockDim.x) {
-        const int u = it / nr, r = it - u * nr;
+        const int u = div_by(it, s_rnr), r = it - u * nr;
         const int pr = s_plist[u];
-        const int pi = pr / pcap;
+        const int pi = div_by(pr, s_rpcap);
         const int s = s_pairslot[pr];
         const int cp = s_pos[s], pp = s_ppos[pi];
         const int cx = cp >> 16, cy = cp & 0xffff, px = pp >> 16, py = pp & 0xffff;
@@ -624,9 +661,9 @@ __global__ void __launch_bounds__(kThreads, 1)
       auto load_item = [&](int it, uint64_t(&w)[4], uint64_t(&x)[5], int &pr, int &fbc) {
         pr = -1;
         if (it >= npair * nr) return;
-        const int u = it / nr, r = it - u * nr;
+        const int u = div_by(it, s_rnr), r = it - u * nr;
         const int pq = s_plist[u];
-        const int pi = pq / pcap;
+        const int pi = div_by(pq, s_rpcap);
         const int s = s_pairslot[pq];
         const int cp = s_pos[s], pp = s_ppos[pi];
         const int cx = cp >> 16, cy = cp & 0xffff, px = pp >> 16, py = pp & 0xffff;
@@ -675,9 +712,9 @@ __global__ void __launch_bounds__(kThreads, 1)
     } else if (nwpr <= 7) {
       // ---- D2. per (pair, row): popcount(placed(c) & N), loads issued together
       for (int it = tid; it < npair * nr; it += blockDim.x) {
-        const int u = it / nr, r = it - u * nr;
+        const int u = div_by(it, s_rnr), r = it - u * nr;
         const int pr = s_plist[u];
-        const int pi = pr / pcap;
+        const int pi = div_by(pr, s_rpcap);
         const int s = s_pairslot[pr];
         const int cp = s_pos[s], pp = s_ppos[pi];
         const int cx = cp >> 16, cy = cp & 0xffff, px = pp >> 16, py = pp & 0xffff;
@@ -765,7 +802,7 @@ __global__ void __launch_bounds__(kThreads, 1)
     if (a.intervis) {
       for (int u = tid; u < npair; u += blockDim.x) {
         const int i = s_plist[u];
-        const int j = i / pcap;
+        const int j = div_by(i, s_rpcap);
         const int s = s_pairslot[i];
         if (!(s_flag[s] & kInel) || !(s_paircov[i] & 1)) continue;
         const int c = s * G + k;
@@ -839,8 +876,9 @@ __global__ void __launch_bounds__(kThreads, 1)
     }
     for (int i = tid; i < mcut; i += blockDim.x) {
       const int c = s_pk[i];
-      if (c % G == k) {
-        const int s = c / G;
+      const int cs = div_by(c, s_rG);
+      if (c - cs * G == k) {
+        const int s = cs;
         s_flag[s] |= kUsed;
         s_dirty[s >> 5] = 1;
         a.selected[c] = 1;
@@ -849,7 +887,7 @@ __global__ void __launch_bounds__(kThreads, 1)
     }
     for (int u = tid; u < npair; u += blockDim.x) {
       const int i = s_plist[u];
-      if (i / pcap >= mcut) continue;
+      if (div_by(i, s_rpcap) >= mcut) continue;
       const int s = s_pairslot[i];
       atomicAdd(&s_dacc[s], s_pairdelta[i]);
       const unsigned char cv = s_paircov[i];
@@ -858,10 +896,10 @@ __global__ void __launch_bounds__(kThreads, 1)
     }
     // coverage: OR this CTA's rows of the accepted picks' placed sheds
     {
-      const int rows_mine = k < nr ? (nr - k + G - 1) / G : 0;
+      const unsigned long long rrb = s_rrows, rnb = s_rnb2;
       for (int i = tid; i < mcut * rows_mine * nb2; i += blockDim.x) {
-        const int pi = i / (rows_mine * nb2), rem = i - pi * rows_mine * nb2;
-        const int prow = k + G * (rem / nb2), j = rem % nb2;
+        const int q = div_by(i, rnb), j = i - q * nb2;  // q = pick*rows_mine + own row
+        const int pi = div_by(q, rrb), prow = k + G * (q - pi * rows_mine);
         const int pos = s_ppos[pi];
         const int px = pos >> 16, py = pos & 0xffff;
         int fwp, fbp;
@@ -876,7 +914,7 @@ __global__ void __launch_bounds__(kThreads, 1)
     __syncthreads();
     for (int u = tid; u < npair; u += blockDim.x) {
       const int i = s_plist[u];
-      if (i / pcap >= mcut) continue;
+      if (div_by(i, s_rpcap) >= mcut) continue;
       const int s = s_pairslot[i];
       const unsigned char tag = s_tag[s];
       if (!(tag & 1)) continue;  // already applied through another pair
@@ -910,7 +948,7 @@ __global__ void __launch_bounds__(kThreads, 1)
     a.out[0] = npicks;
     a.out[1] = s_cum;
     a.out[2] = rounds;
-    for (int i = 0; i < kSitePhases; i++) a.out[3 + i] = ph[i];
+    for (int i = 0; i < kSitePhases; i++) a.out[3 + i] = s_ph[i];
   }
 }
 
