@@ -452,6 +452,10 @@ __global__ void __launch_bounds__(kThreads, 1)
     // depends on m only, so all CTAs make it alike.
     const bool dist = m * nr > (int)blockDim.x || nwpr > 7 ||
                       m * nr * nb2 > a.ncap_words;
+    // A large round also keeps this CTA's own new-bit rows in the (otherwise
+    // unused) shared buffer, item i of the spread rows at words i*nb2..: the
+    // coverage update ORs them (cum | placed = cum | (placed & ~cum)).
+    const bool own_n = dist && m * rows_mine * nb2 <= a.ncap_words;
     // ---- D1 (spread): this CTA's rows of every pick, popcounts for the
     // self-check
     if (dist) {
@@ -484,6 +488,7 @@ __global__ void __launch_bounds__(kThreads, 1)
             const uint64_t v =
                 ((w[q] >> fbp) | ((q > 0 && fbp) ? w[q - 1] << (64 - fbp) : 0ull)) & ~x[q];
             __stcg(nrow + q, v);
+            if (own_n) s_N[(size_t)i * nb2 + q] = v;
             cnt += __popcll(v);
           }
         } else {
@@ -493,6 +498,7 @@ __global__ void __launch_bounds__(kThreads, 1)
             if (row_in && W >= 0 && W < cw)
               v = placed_word(prw, j, nwpr, fbp) & ~__ldcg(cum + (size_t)gr * cw + W);
             __stcg(nrow + j, v);
+            if (own_n) s_N[(size_t)i * nb2 + j] = v;
             cnt += __popcll(v);
           }
         }
@@ -906,8 +912,11 @@ __global__ void __launch_bounds__(kThreads, 1)
         shed_align(py - roi, fwp, fbp);
         const int gr = px - roi + prow, W = fwp + j;
         if (gr < 0 || gr >= n || W < 0 || W >= cw) continue;
+        // the pick's new bits where this CTA holds them, else its placed shed
         const uint64_t v =
-            placed_word(a.sheds + (size_t)s_pk[pi] * per + (size_t)prow * nwpr, j, nwpr, fbp);
+            own_n ? s_N[i]
+            : !dist ? s_N[(size_t)(pi * nr + prow) * nb2 + j]
+                    : placed_word(a.sheds + (size_t)s_pk[pi] * per + (size_t)prow * nwpr, j, nwpr, fbp);
         if (v) atomicOr(reinterpret_cast<unsigned long long *>(cum + (size_t)gr * cw + W), v);
       }
     }

@@ -55,11 +55,15 @@ struct ShedArgs {
 // DEM accessors by linear offset: `base` is the observer cell's offset, a cell
 // (dx, dy) away is at base + dx*stride + dy.
 struct SmemDem {
-  const uint16_t *s;
+  uint32_t s;  // shared-memory address of the window
   int w, x0, y0;
   __device__ __forceinline__ int base(int x, int y) const { return (x - x0) * w + (y - y0); }
   __device__ __forceinline__ int stride() const { return w; }
-  __device__ __forceinline__ int at(int o) const { return s[o]; }
+  __device__ __forceinline__ int at(int o) const {
+    unsigned short v;
+    asm("ld.shared.u16 %0, [%1];" : "=h"(v) : "r"(s + 2u * (uint32_t)o));
+    return v;
+  }
 };
 
 struct GlobalDem {
@@ -90,7 +94,7 @@ __device__ __forceinline__ void mark_row_major(const ShedImage &im, int row, int
 
 template <bool kRcp, class Dem>
 __device__ __forceinline__ void sweep_rays(const Dem &dem, const ShedArgs &a, int ox, int oy,
-                                           const ShedImage &im, const float *rcp) {
+                                           const ShedImage &im, uint32_t rcp) {
   const int roi = a.roi, n = a.n, side = 2 * roi;
   const int roi2 = roi * roi;
   const int xmin = ox - roi, ymin = oy - roi, xmax = ox + roi, ymax = oy + roi;
@@ -141,7 +145,7 @@ __device__ __forceinline__ void sweep_rays(const Dem &dem, const ShedArgs &a, in
     // y-major rays mark the row-major image (line = row), x-major rays the
     // column-major one (line = column); pos is the cell's coordinate along
     // the ray's axis, bit pos%32 of word line*stride + pos/32
-    unsigned *img = my ? im.R : im.C;
+    const uint32_t img = smem_u32(my ? im.R : im.C);  // shared-memory address
     const int stride = my ? im.rs : im.cs;
     int pb = obase, pos = roi;
     const float fend = i2f(kend);
@@ -161,7 +165,8 @@ __device__ __forceinline__ void sweep_rays(const Dem &dem, const ShedArgs &a, in
       if (t <= fa) {
         float s;
         if (kRcp) {
-          const float y = rcp[__float2int_rz(fai)];
+          float y;
+          asm("ld.shared.f32 %0, [%1];" : "=f"(y) : "r"(rcp + 4u * (uint32_t)__float2int_rz(fai)));
           const float q0 = __fmul_rn(fa, y);
           s = __fmaf_rn(__fmaf_rn(-q0, fai, fa), y, q0);
         } else {
@@ -175,7 +180,8 @@ __device__ __forceinline__ void sweep_rays(const Dem &dem, const ShedArgs &a, in
       // pelev + tht against oalt + hs*|i|: both sums in one packed add
       const unsigned long long V = f2_add(f2_pack(fe, foalt), f2_pack(ftht, t));
       if (f2_lo(V) >= f2_hi(V))
-        atomicOr(&img[(off + roi) * stride + (pos >> 5)], 1u << (pos & 31));
+        asm volatile("red.shared.or.b32 [%0], %1;" ::"r"(img + 4u * (uint32_t)((off + roi) * stride + (pos >> 5))),
+                     "r"(1u << (pos & 31)) : "memory");
     }
   }
 }
@@ -223,9 +229,9 @@ __device__ __forceinline__ void shed_body(const CUtensorMap &map, const ShedArgs
       if (threadIdx.x == 0) atomicOr(a.err, kErrTmaTimeout);
       return;
     }
-    sweep_rays<kRcp>(SmemDem{win, a.win_w, hx0, hy0}, a, ox, oy, im, rcp);
+    sweep_rays<kRcp>(SmemDem{smem_u32(win), a.win_w, hx0, hy0}, a, ox, oy, im, smem_u32(rcp));
   } else {
-    sweep_rays<kRcp>(GlobalDem{a.dem, a.pitch}, a, ox, oy, im, rcp);
+    sweep_rays<kRcp>(GlobalDem{a.dem, a.pitch}, a, ox, oy, im, smem_u32(rcp));
   }
   __syncthreads();
   // fold C into R: one warp per 32x32 block; lane j holds column cb*32+j's
