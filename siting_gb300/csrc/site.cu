@@ -58,6 +58,7 @@ int site_threads_for(int nslots, int roi) { return (nslots > 1024 || roi > 127) 
 constexpr int kMaxSlots = 4096;  // candidates owned by one CTA
 constexpr int kTopK = 4;         // keys each CTA publishes per round
 constexpr int kMaxPicks = 64;    // picks accepted in one round at most
+constexpr int kSmallRecip = 128; // reciprocals tabled in shared memory (>= kMaxPicks)
 constexpr int kMaxPairs = 8192;  // (candidate, pick) pairs one CTA updates per round
 
 struct SiteArgs {
@@ -168,6 +169,7 @@ __global__ void __launch_bounds__(kThreads, 1)
   // reciprocals (div_recip) of the kernel's divisors and of each pick's run
   __shared__ unsigned long long s_rG, s_rnr, s_rpcap, s_rm, s_rrows, s_rnb2;
   __shared__ unsigned long long s_rrun[kMaxPicks];
+  __shared__ unsigned long long s_rsmall[kSmallRecip + 1];  // div_recip(d), d <= kSmallRecip
   __shared__ int4 s_pbox[kMaxPicks];  // per pick: start of its first block row, run, per_run, items
   __shared__ unsigned long long s_red[32];
   __shared__ int s_rank[kMaxPicks], s_rpos[kMaxPicks];
@@ -184,6 +186,7 @@ __global__ void __launch_bounds__(kThreads, 1)
   const int GK = G * kTopK;
   const int pcap = a.pick_cap;
   const int rows_mine = k < nr ? (nr - k + G - 1) / G : 0;  // coverage rows this CTA owns
+  for (int d = tid; d <= kSmallRecip; d += blockDim.x) s_rsmall[d] = div_recip(max(d, 1));
   if (tid == 0) {
     s_rG = div_recip(G);
     s_rnr = div_recip(nr);
@@ -430,13 +433,13 @@ __global__ void __launch_bounds__(kThreads, 1)
           const int run = (byh - byl + 1) * a.npb;
           const int per_run = run / G + 2;
           s_pbox[j] = make_int4((bxl * a.nb + byl) * a.npb, run, per_run, (bxh - bxl + 1) * per_run);
-          s_rrun[j] = div_recip(per_run);
+          s_rrun[j] = per_run <= kSmallRecip ? s_rsmall[per_run] : div_recip(per_run);
         }
       }
       if (lane == 0) {
         s_m = m;
         s_stop_at = stop_at;
-        s_rm = div_recip(max(m, 1));
+        s_rm = s_rsmall[max(m, 1)];  // m <= kMaxPicks <= kSmallRecip
       }
     }
     __syncthreads();
