@@ -70,11 +70,17 @@ int plan_batch(int sm_count, int njobs, const siting_params *params, const sitin
     J.auto_G = !(pl && pl->site_ctas > 0);
     if (!site_fits(J, J.G)) return bad(j, "SITE shared-memory plan too large");
   }
-  // SITE launches: pack the groups, largest first, into waves of <= sm_count CTAs
+  // SITE launches: pack the groups into waves of <= sm_count CTAs, intervis
+  // jobs first (their selections take several times more rounds), largest
+  // groups first within each kind.  Waves run in order, each as soon as its
+  // jobs' viewsheds exist, so the long selections overlap later jobs' stages
+  // and the last wave, which nothing overlaps, holds the short ones.
   std::vector<int> order(njobs);
   std::iota(order.begin(), order.end(), 0);
-  std::stable_sort(order.begin(), order.end(),
-                   [&](int a, int b) { return jobs[a].G > jobs[b].G; });
+  std::stable_sort(order.begin(), order.end(), [&](int a, int b) {
+    if (jobs[a].p.intervis != jobs[b].p.intervis) return jobs[a].p.intervis > jobs[b].p.intervis;
+    return jobs[a].G > jobs[b].G;
+  });
   std::vector<std::vector<int>> &waves = bp->waves;
   std::vector<int> &wave_ctas = bp->wave_ctas;
   waves.clear();
