@@ -55,6 +55,7 @@ struct ShedArgs {
 // DEM accessors by linear offset: `base` is the observer cell's offset, a cell
 // (dx, dy) away is at base + dx*stride + dy.
 struct SmemDem {
+  static constexpr bool kShared = true;
   uint32_t s;  // shared-memory address of the window
   int w, x0, y0;
   __device__ __forceinline__ int base(int x, int y) const { return (x - x0) * w + (y - y0); }
@@ -67,6 +68,7 @@ struct SmemDem {
 };
 
 struct GlobalDem {
+  static constexpr bool kShared = false;
   const uint16_t *g;
   int pitch;
   __device__ __forceinline__ int base(int x, int y) const { return x * pitch + y; }
@@ -152,36 +154,62 @@ __device__ __forceinline__ void sweep_rays(const Dem &dem, const ShedArgs &a, in
     // elevations and offsets are integers below 2^24: their differences and
     // sums are exact in FP32, so (float)(pelev - oalt) = pelev_f - foalt
     float hs = -99999.f;
-    for (float fai = 1.f; fai <= fend; fai = fadd(fai, 1.f)) {  // fai = (float)|i|, exact
-      pb += smaj;
-      pos += dir;
-      const int off = round_i(fmul(fai, sl));
-      const float fe = i2f(dem.at(pb + off * smin));
-      const float fa = __fsub_rn(fe, foalt);
-      // s = RN(a/|i|) can exceed hs only if a > hs*|i|, and then t = RN(hs*|i|)
-      // <= a (rounding is monotone and a is a float): the division runs only
-      // when the horizon may rise, and t serves the visibility test as well
-      float t = fmul(hs, fai);
-      if (t <= fa) {
-        float s;
-        if (kRcp) {
-          float y;
-          asm("ld.shared.f32 %0, [%1];" : "=f"(y) : "r"(rcp + 4u * (uint32_t)__float2int_rz(fai)));
-          const float q0 = __fmul_rn(fa, y);
-          s = __fmaf_rn(__fmaf_rn(-q0, fai, fa), y, q0);
-        } else {
-          s = fdiv(fa, fai);
-        }
-        if (hs < s) {
-          hs = s;
-          t = fmul(hs, fai);
-        }
+    if (kRcp && Dem::kShared) {
+      // The table division costs a few instructions: every step divides and
+      // takes the larger slope (s > hs ? s : hs, the reference's update),
+      // with no branch for the lanes of a warp to diverge on (window in
+      // shared memory; through L1 the extra table read per step costs more).
+      uint32_t rp = rcp + 4u;  // &rcp[|i|]
+      for (float fai = 1.f; fai <= fend; fai = fadd(fai, 1.f)) {  // fai = (float)|i|, exact
+        pb += smaj;
+        pos += dir;
+        const int off = round_i(fmul(fai, sl));
+        const float fe = i2f(dem.at(pb + off * smin));
+        const float fa = __fsub_rn(fe, foalt);
+        float y;
+        asm("ld.shared.f32 %0, [%1];" : "=f"(y) : "r"(rp));
+        rp += 4u;
+        const float q0 = __fmul_rn(fa, y);
+        const float sn = __fmaf_rn(__fmaf_rn(-q0, fai, fa), y, q0);
+        hs = hs < sn ? sn : hs;
+        const float t = fmul(hs, fai);
+        // pelev + tht against oalt + hs*|i|: both sums in one packed add
+        const unsigned long long V = f2_add(f2_pack(fe, foalt), f2_pack(ftht, t));
+        if (f2_lo(V) >= f2_hi(V))
+          asm volatile("red.shared.or.b32 [%0], %1;" ::"r"(img + 4u * (uint32_t)((off + roi) * stride + (pos >> 5))),
+                       "r"(1u << (pos & 31)) : "memory");
       }
-      // pelev + tht against oalt + hs*|i|: both sums in one packed add
-      const unsigned long long V = f2_add(f2_pack(fe, foalt), f2_pack(ftht, t));
-      if (f2_lo(V) >= f2_hi(V))
-        asm volatile("red.shared.or.b32 [%0], %1;" ::"r"(img + 4u * (uint32_t)((off + roi) * stride + (pos >> 5))),
-                     "r"(1u << (pos & 31)) : "memory");
+    } else {
+      for (float fai = 1.f; fai <= fend; fai = fadd(fai, 1.f)) {  // fai = (float)|i|, exact
+        pb += smaj;
+        pos += dir;
+        const int off = round_i(fmul(fai, sl));
+        const float fe = i2f(dem.at(pb + off * smin));
+        const float fa = __fsub_rn(fe, foalt);
+        // s = RN(a/|i|) can exceed hs only if a > hs*|i|, and then t = RN(hs*|i|)
+        // <= a (rounding is monotone and a is a float): the division runs only
+        // when the horizon may rise, and t serves the visibility test as well
+        float t = fmul(hs, fai);
+        if (t <= fa) {
+          float sn;
+          if (kRcp) {
+            float y;
+            asm("ld.shared.f32 %0, [%1];" : "=f"(y) : "r"(rcp + 4u * (uint32_t)__float2int_rz(fai)));
+            const float q0 = __fmul_rn(fa, y);
+            sn = __fmaf_rn(__fmaf_rn(-q0, fai, fa), y, q0);
+          } else {
+            sn = fdiv(fa, fai);
+          }
+          if (hs < sn) {
+            hs = sn;
+            t = fmul(hs, fai);
+          }
+        }
+        const unsigned long long V = f2_add(f2_pack(fe, foalt), f2_pack(ftht, t));
+        if (f2_lo(V) >= f2_hi(V))
+          asm volatile("red.shared.or.b32 [%0], %1;" ::"r"(img + 4u * (uint32_t)((off + roi) * stride + (pos >> 5))),
+                       "r"(1u << (pos & 31)) : "memory");
+      }
     }
   }
 }
