@@ -42,6 +42,7 @@ struct VixArgs {
 // DEM accessors by linear offset: `base` is the observer cell's offset, a cell
 // (dx, dy) away is at base + dx*stride + dy.
 struct SmemDem {
+  static constexpr bool kShared = true;
   const uint16_t *s;
   int w, x0, y0;
   __device__ __forceinline__ int base(int x, int y) const { return (x - x0) * w + (y - y0); }
@@ -50,6 +51,7 @@ struct SmemDem {
 };
 
 struct GlobalDem {
+  static constexpr bool kShared = false;
   const uint16_t *g;
   int pitch;
   __device__ __forceinline__ int base(int x, int y) const { return x * pitch + y; }
@@ -99,6 +101,21 @@ __device__ __forceinline__ int vix_target(const Dem &dem, int obase, int n, int 
   const unsigned long long C = f2_pack(round_addend(f2_lo(P)), foz);  // the sign never changes
   const int smin = mx ? 1 : W;
   int q = obase + (mx ? (d > 0 ? W : -W) : (d > 0 ? 1 : -1));  // observer + id*(major stride)
+  if (Dem::kShared) {
+    // With the halo in shared memory every sample is tested: a blocked
+    // target's lane would idle until its warp's other lanes finish anyway, and
+    // no branch is left for the lanes to diverge on.  (Through L1 the extra
+    // loads cost more than the branch.)
+    bool vis = true;
+    for (int step = 1; step < ad; step <<= 1) {
+      const unsigned long long Q = f2_add(P, C);
+      const int off = f2i(f2_lo(Q));  // round(slope*id), half away from zero
+      vis &= !(i2f(dem.at(q + off * smin)) > f2_hi(Q));
+      P = f2_add(P, P);
+      q = 2 * q - obase;  // id doubles
+    }
+    return vis;
+  }
   for (int step = 1; step < ad; step <<= 1) {
     const unsigned long long Q = f2_add(P, C);
     const int off = f2i(f2_lo(Q));  // round(slope*id), half away from zero
