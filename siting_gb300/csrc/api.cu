@@ -222,11 +222,12 @@ int sheds_dev(siting_ctx *ctx, const DemView &dem, int roi, int oht, int tht, in
   return SITING_OK;
 }
 
-int site_ctas_for(siting_ctx *ctx, int roi, int nsheds) {
+int site_ctas_for(siting_ctx *ctx, int roi, int nsheds, int nb, int npb, float bs) {
   const siting_plan *tp = tuned_plan(ctx, roi, -1);
-  int G = ctx->site_ctas > 0          ? ctx->site_ctas
-          : tp && tp->site_ctas > 0   ? std::max(tp->site_ctas, (nsheds + 4095) / 4096)
-                                      : site_default_ctas(nsheds, ctx->sm_count);
+  int G = ctx->site_ctas > 0        ? ctx->site_ctas
+          : tp && tp->site_ctas > 0 ? std::max(tp->site_ctas, (nsheds + 4095) / 4096)
+                                    : site_spread_ctas(site_default_ctas(nsheds, ctx->sm_count), roi,
+                                                       nsheds, nb, npb, bs, ctx->sm_count);
   return std::min(G, ctx->sm_count);
 }
 
@@ -238,7 +239,7 @@ int site_enqueue(siting_ctx *ctx, int nrows, int roi, int intervis, int nsheds,
   if (!ctx->h_out) CK(cudaMallocHost(&ctx->h_out, 16 * sizeof(long long)));
   memset(ctx->h_out, 0, 16 * sizeof(long long));
   if (nsheds <= 0) return SITING_OK;
-  const int G = site_ctas_for(ctx, roi, nsheds);
+  const int G = site_ctas_for(ctx, roi, nsheds, nb, npb, bs);
   if (!site_supported(roi, nsheds, G))
     return fail(ctx, SITING_EINVAL, "SITE: roi or nsheds beyond the device kernel's limits");
   if (site_smem_bytes(roi, nsheds, G, nb, npb, bs) > 220 * 1024)

@@ -111,6 +111,9 @@ cudaError_t launch_site_jobs(const SiteJob *jobs, int njobs, void *d_table, void
 size_t site_scratch_bytes(int nrows, int nsheds, int nctas, int roi);
 void site_carve_scratch(void *base, int nrows, int nsheds, int nctas, int roi, SiteScratch *s);
 int site_default_ctas(int nsheds, int sm_count);
+// The CTA count near G0 that spreads a pick's neighbourhood most evenly over
+// the CTAs for the job's block geometry (nb blocks a row, npb candidates each).
+int site_spread_ctas(int G0, int roi, int nsheds, int nb, int npb, float bs, int sm_count);
 // Smallest covered-cell count at which the reference's 95% stop test holds.
 long long site_stop_area(int nrows);
 size_t site_smem_bytes(int roi, int nsheds, int nctas, int nblocks, int npb, float blocksize);

@@ -1069,6 +1069,52 @@ int site_default_ctas(int nsheds, int sm_count) {
   return std::min(g, std::min(sm_count, 160));
 }
 
+// Candidate c belongs to CTA c % G, and candidates are numbered block-major
+// ((block row * nb + block column) * npb + k), so a pick's neighbour search
+// (span block rows of span*npb consecutive indices, the FINDMAX geometry) lands
+// on CTAs (r * nb * npb + w) % G.  When nb*npb shares a large factor with G
+// the rows fall on the same few CTAs (1000^2, nb = 100: at G = 100 every CTA
+// owns one block column, and a round's pairs sit on ~27 of the 100 CTAs).
+// Among G within a quarter of the default, take the one whose busiest CTA owns
+// the fewest indices of such a rectangle, the nearest to the default on ties.
+int site_spread_ctas(int G0, int roi, int nsheds, int nb, int npb, float bs, int sm_count) {
+  const int span = std::min(nb, (int)std::ceil((4.0 * roi + 1.0) / bs) + 6);
+  const long long stride = (long long)nb * npb, W = (long long)span * npb;
+  const int lo = std::max({1, (G0 * 3) / 4, (nsheds + kMaxSlots - 1) / kMaxSlots});
+  const int hi = std::min({sm_count, 160, (G0 * 5) / 4});
+  auto busiest = [&](int G) {
+    std::vector<int> diff(G + 1, 0);
+    long long all = 0;
+    for (int r = 0; r < span; r++) {  // row r covers W consecutive residues from r*stride
+      const int start = (int)((r * stride) % G);
+      all += W / G;
+      const int rem = (int)(W % G);
+      if (rem == 0) continue;
+      diff[start]++;
+      if (start + rem <= G) {
+        diff[start + rem]--;
+      } else {
+        diff[G]--;
+        diff[0]++;
+        diff[start + rem - G]--;
+      }
+    }
+    int run = 0, mx = 0;
+    for (int g = 0; g < G; g++) mx = std::max(mx, run += diff[g]);
+    return all + mx;
+  };
+  int best = G0;
+  long long bw = G0 >= lo && G0 <= hi ? busiest(G0) : (long long)1 << 62;
+  for (int G = lo; G <= hi; G++) {
+    const long long w = busiest(G);
+    if (w < bw || (w == bw && std::abs(G - G0) < std::abs(best - G0))) {
+      bw = w;
+      best = G;
+    }
+  }
+  return best;
+}
+
 namespace {
 
 // Shared memory of everything but the new-bits buffer.
