@@ -862,8 +862,12 @@ __global__ void __launch_bounds__(kThreads, 1)
       if (tid == 0) __stcg(a.cuts + par * G + k, s_roundcut);
     }
     mark(12);
-    // every read of the coverage this round is done once all CTAs pass here
-    if (!group_sync(gb, a.err, &s_flagv)) return;
+    // every read of the coverage this round is done once all CTAs pass here.
+    // Without intervis there is no cut to agree on, and in a spread round the
+    // coverage is read only before the spread barrier: the coverage update
+    // may start at once.  (The buffers reused by the next round are written
+    // only after its first barrier, which every CTA reaches after this one.)
+    if ((a.intervis || !dist) && !group_sync(gb, a.err, &s_flagv)) return;
     if (tid == 0) s_mcut = m;
     __syncthreads();
     if (a.intervis) {  // the smallest cut of any CTA: one load per thread
