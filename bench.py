@@ -302,13 +302,13 @@ def stage_bytes(w, nwanted, site_bytes):
 # DRAM bytes per launch (dram__bytes_read.sum + dram__bytes_write.sum) from
 # ncu: VIX, VIEWSHED and SITE captured at full size (profiles/launches_c2_4096.md).
 NCU_TRAFFIC = {
-    "c2_4096": {"vix": 33571072 + 6400, "viewshed": 34218496 + 362720768,
-                "site": 2496145152 + 11676672},
+    "c2_4096": {"vix": 33794048 + 0, "viewshed": 35159296 + 364115200,
+                "site": 2494696192 + 10018048},
 }
 
 ROOFLINE_NOTES = {
     "vix": "VIX is SM-issue bound, not HBM bound: its compulsory traffic is 3 B/cell and ncu shows "
-           "89.8% issue-active cycles, 3.57 warp instructions a cycle of 4 "
+           "88.5% issue-active cycles, 3.54 warp instructions a cycle of 4 "
            "(profiles/vix_kernel_c2_2048.md)",
     "site": "SITE's algorithmic bytes are the reference's rescoring traffic (every rescored "
             "candidate's shed and coverage window per pick); this kernel updates gains by "
