@@ -155,6 +155,8 @@ __device__ __forceinline__ void sweep_rays(const Dem &dem, const ShedArgs &a, in
     // sums are exact in FP32, so (float)(pelev - oalt) = pelev_f - foalt
     float hs = -99999.f;
     if (kRcp && Dem::kShared) {
+      // the sign of |i|*slope is the slope's: round's addend is fixed per ray
+      const float hsl = round_addend(sl);
       // The table division costs a few instructions: every step divides and
       // takes the larger slope (s > hs ? s : hs, the reference's update),
       // with no branch for the lanes of a warp to diverge on (window in
@@ -163,7 +165,7 @@ __device__ __forceinline__ void sweep_rays(const Dem &dem, const ShedArgs &a, in
       for (float fai = 1.f; fai <= fend; fai = fadd(fai, 1.f)) {  // fai = (float)|i|, exact
         pb += smaj;
         pos += dir;
-        const int off = round_i(fmul(fai, sl));
+        const int off = f2i(fadd(fmul(fai, sl), hsl));  // round(|i|*slope), half away from zero
         const float fe = i2f(dem.at(pb + off * smin));
         const float fa = __fsub_rn(fe, foalt);
         float y;
