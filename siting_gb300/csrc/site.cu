@@ -13,12 +13,12 @@
 //
 // GB300 mapping: one persistent kernel of G co-resident CTAs (one per SM)
 // with a bounded group barrier.  Candidate c is owned by CTA c % G, which
-// keeps its true gain, area, cell and flags in shared memory and a top-4 key
-// list per 32 slots (key = area << 32 | ~c).  A round:
-//   A. every CTA publishes its own top-4 keys; one barrier;
+// keeps its true gain, area, cell and flags in shared memory and a top-K key
+// list per 32 slots (key = area << 32 | ~c, K = kTopK).  A round:
+//   A. every CTA publishes its own top-K keys; one barrier;
 //   B. every CTA merges the G lists identically and accepts the longest
 //      prefix of the global key order whose members are pairwise > 2*roi
-//      apart, up to the exactness threshold (the largest 4th key of any list:
+//      apart, up to the exactness threshold (the largest K-th key of any list:
 //      unpublished keys are below it) and the 95% stop.  A candidate > 2*roi
 //      from every earlier pick of the round keeps its key, every other key
 //      can only fall, so the prefix equals the sequential greedy's next picks;
@@ -56,7 +56,11 @@ namespace {
 // sheds (measured: 4096^2/roi 100 9.9 vs 10.2 ms; 16384^2/roi 200 88.8 vs 77.8 ms).
 int site_threads_for(int nslots, int roi) { return (nslots > 1024 || roi > 127) ? 1024 : 512; }
 constexpr int kMaxSlots = 4096;  // candidates owned by one CTA
-constexpr int kTopK = 4;         // keys each CTA publishes per round
+// Keys each CTA publishes per round.  Rounds end at distance conflicts and
+// intervis cuts long before the threshold of K keys binds (4096^2: 343
+// rounds with 3, 4, 6 or 8), and fewer keys make each merge cheaper; with 2
+// the threshold binds (16384^2: 725 -> 1015 rounds).
+constexpr int kTopK = 3;
 constexpr int kMaxPicks = 64;    // picks accepted in one round at most
 constexpr int kSmallRecip = 128; // reciprocals tabled in shared memory (>= kMaxPicks)
 constexpr int kMaxPairs = 8192;  // (candidate, pick) pairs one CTA updates per round
