@@ -302,8 +302,8 @@ def stage_bytes(w, nwanted, site_bytes):
 # DRAM bytes per launch (dram__bytes_read.sum + dram__bytes_write.sum) from
 # ncu: VIX, VIEWSHED and SITE captured at full size (profiles/launches_c2_4096.md).
 NCU_TRAFFIC = {
-    "c2_4096": {"vix": 33794048 + 0, "viewshed": 35159296 + 364115200,
-                "site": 2494696192 + 10018048},
+    "c2_4096": {"vix": 33720064 + 1536, "viewshed": 34480896 + 365585152,
+                "site": 2494835712 + 10062080},
 }
 
 ROOFLINE_NOTES = {
