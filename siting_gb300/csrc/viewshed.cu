@@ -154,7 +154,7 @@ __device__ __forceinline__ void sweep_rays(const Dem &dem, const ShedArgs &a, in
     // elevations and offsets are integers below 2^24: their differences and
     // sums are exact in FP32, so (float)(pelev - oalt) = pelev_f - foalt
     float hs = -99999.f;
-    if (kRcp && Dem::kShared) {
+    if constexpr (kRcp && Dem::kShared) {
       // the sign of |i|*slope is the slope's: round's addend is fixed per ray
       const float hsl = round_addend(sl);
       // The table division costs a few instructions: every step divides and

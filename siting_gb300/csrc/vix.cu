@@ -101,7 +101,7 @@ __device__ __forceinline__ int vix_target(const Dem &dem, int obase, int n, int 
   const unsigned long long C = f2_pack(round_addend(f2_lo(P)), foz);  // the sign never changes
   const int smin = mx ? 1 : W;
   int q = obase + (mx ? (d > 0 ? W : -W) : (d > 0 ? 1 : -1));  // observer + id*(major stride)
-  if (Dem::kShared) {
+  if constexpr (Dem::kShared) {
     // With the halo in shared memory every sample is tested: a blocked
     // target's lane would idle until its warp's other lanes finish anyway, and
     // no branch is left for the lanes to diverge on.  (Through L1 the extra
@@ -115,15 +115,16 @@ __device__ __forceinline__ int vix_target(const Dem &dem, int obase, int n, int 
       q = 2 * q - obase;  // id doubles
     }
     return vis;
+  } else {
+    for (int step = 1; step < ad; step <<= 1) {
+      const unsigned long long Q = f2_add(P, C);
+      const int off = f2i(f2_lo(Q));  // round(slope*id), half away from zero
+      if (i2f(dem.at(q + off * smin)) > f2_hi(Q)) return 0;
+      P = f2_add(P, P);
+      q = 2 * q - obase;  // id doubles
+    }
+    return 1;
   }
-  for (int step = 1; step < ad; step <<= 1) {
-    const unsigned long long Q = f2_add(P, C);
-    const int off = f2i(f2_lo(Q));  // round(slope*id), half away from zero
-    if (i2f(dem.at(q + off * smin)) > f2_hi(Q)) return 0;
-    P = f2_add(P, P);
-    q = 2 * q - obase;  // id doubles
-  }
-  return 1;
 }
 
 // The tile's (cell, target) items: L = blockDim/T^2 consecutive threads share
