@@ -1086,6 +1086,7 @@ int site_default_ctas(int nsheds, int sm_count) {
 // Among G within a quarter of the default, take the one whose busiest CTA owns
 // the fewest indices of such a rectangle, the nearest to the default on ties.
 int site_spread_ctas(int G0, int roi, int nsheds, int nb, int npb, float bs, int sm_count) {
+  if (nb <= 1) return G0;  // candidates in one run (no block geometry): nothing to spread
   const int span = std::min(nb, (int)std::ceil((4.0 * roi + 1.0) / bs) + 6);
   const long long stride = (long long)nb * npb, W = (long long)span * npb;
   const int lo = std::max({1, (G0 * 3) / 4, (nsheds + kMaxSlots - 1) / kMaxSlots});
