@@ -50,10 +50,11 @@
 namespace siting {
 namespace {
 
-// Threads a CTA: 512 allow 128 registers a thread (no spills) and suit jobs
-// with few candidates per CTA and narrow sheds; 1024 (64 registers, a few
-// spills) keep more items in flight for many candidates per CTA or wide
-// sheds (measured: 4096^2/roi 100 9.9 vs 10.2 ms; 16384^2/roi 200 88.8 vs 77.8 ms).
+// Threads a CTA: 512 allow 128 registers a thread and suit jobs with few
+// candidates per CTA and narrow sheds; 1024 (64 registers) keep more items
+// in flight for many candidates per CTA or wide sheds (measured, SITE ms at
+// 512 and 1024 threads: 4096^2/roi 100 7.41 vs 7.65; 16384^2/roi 200 51.5 vs
+// 42.7).
 int site_threads_for(int nslots, int roi) { return (nslots > 1024 || roi > 127) ? 1024 : 512; }
 constexpr int kMaxSlots = 4096;  // candidates owned by one CTA
 // Keys each CTA publishes per round.  Rounds end at distance conflicts and
