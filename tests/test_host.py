@@ -152,3 +152,20 @@ def test_server_refuses_without_device(native):
     with pytest.raises(native.SitingError) as e:
         native.Server(0, hbm_budget=1 << 30)
     assert e.value.status == native.EDEVICE
+
+
+def test_noalloc_site_checks_arguments_on_the_host(native):
+    """The allocation-free SITE entry point rejects bad arguments before any
+    device work, and an empty job succeeds without touching a device."""
+    import ctypes as C
+
+    lib = native.load()
+    res = native._ResultC()
+    res.nusedsheds = 99
+    buf = C.c_void_p(16)  # never dereferenced: every call below returns first
+    for args in [(0, 10, 0, 1), (20001, 10, 0, 1), (100, 0, 0, 1), (100, 10, 2, 1),
+                 (100, 10, 0, -1)]:
+        assert lib.siting_site_it_noalloc(*args, buf, buf, buf, None, C.byref(res)) == 1
+    assert lib.siting_site_it_noalloc(100, 10, 0, 5, None, buf, buf, None, C.byref(res)) == 1
+    assert lib.siting_site_it_noalloc(100, 10, 1, 0, None, None, None, None, C.byref(res)) == 0
+    assert (res.nusedsheds, res.cumarea, res.site_rounds) == (0, 0, 0)
