@@ -162,6 +162,7 @@ __device__ __forceinline__ void sweep_rays(const Dem &dem, const ShedArgs &a, in
       // with no branch for the lanes of a warp to diverge on (window in
       // shared memory; through L1 the extra table read per step costs more).
       uint32_t rp = rcp + 4u;  // &rcp[|i|]
+#pragma unroll 2  // two steps a trip: half the loop tests and branches
       for (float fai = 1.f; fai <= fend; fai = fadd(fai, 1.f)) {  // fai = (float)|i|, exact
         pb += smaj;
         pos += dir;
