@@ -12,9 +12,12 @@ download inside the timed region).  Between timed steps the L2 is flushed by
 writing a 512 MiB buffer.  Under torchrun each rank runs an independent
 replica (its own DEM seed): value = all ranks' cells / max rank time.
 
-`--impl reference` times the CPU implementation of the same pipeline (the
-reference built from its sources where available, else the oracle port) on
-the host's cores, on a bounded sample of the workload.
+`--impl reference` times the reference's own CPU implementation (siting.cpp
+built with OpenMP from its staged sources, in library form, every host
+thread) on the same whole workload, without loading this library; its line
+also carries one run of `ompsite` as the reference's makefile builds it
+(50 threads, hard-coded).  The default line's `cpu_baseline` is one whole
+job of the same library-form run.
 """
 from __future__ import annotations
 
@@ -41,6 +44,9 @@ WORKLOADS = {
                     intervis=0, octaves=8, ridged=0.0, range_max=10000, seed=1000),
     "c4_16384": dict(nrows=16384, roi=200, height=150, ntests=64, bw=32, nwanted0=262144,
                      intervis=0, octaves=12, ridged=0.0, range_max=40000, seed=16384),
+    # a small job for quick checks of the harness itself
+    "fbm_256": dict(nrows=256, roi=20, height=30, ntests=32, bw=16, nwanted0=256,
+                    intervis=1, octaves=7, ridged=0.0, range_max=5000, seed=256),
 }
 METRIC = "DEM cells/s end-to-end"
 
@@ -266,8 +272,8 @@ def run_gpu(args, w):
         "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": mean_dev, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32/u64", "data": "synthetic",
-        "config": dict(workload_config(args, w, world, g.nwanted),
-                       plan="autotuned " + str(tuned) if tuned else "library default"),
+        "config": workload_config(args, w, world, g.nwanted),
+        "plan": "autotuned " + str(tuned) if tuned else "library default",
         "e2e": {"value": world * n * n / (mean_e2e / 1e3), "unit": "cells/s",
                 "ms_per_step": mean_e2e, "h2d_bytes_per_step": n * n * 2,
                 "d2h_bytes_per_step": g.nwanted * 5},
@@ -300,28 +306,40 @@ def stage_bytes(w, nwanted, site_bytes):
 
 
 # DRAM bytes per launch (dram__bytes_read.sum + dram__bytes_write.sum) from
-# ncu: VIX, VIEWSHED and SITE captured at full size (profiles/launches_c2_4096.md).
+# ncu: VIX, VIEWSHED and SITE captured at full size (4096^2 launch list).
 NCU_TRAFFIC = {
     "c2_4096": {"vix": 33720064 + 1536, "viewshed": 34480896 + 365585152,
                 "site": 2494835712 + 10062080},
 }
 
+# Warp instructions per unit of work of the two issue-bound stages, from ncu
+# (smsp__inst_executed.sum of one launch / its units) on the 2048^2 capture
+# with roi 100 and 100 targets: per target for VIX, per observer for
+# VIEWSHED.  Keyed by the parameters they were measured with.
+ISSUE_WORK = {
+    ("vix", 100, 100): (2.10e9 / (2048 * 2048 * 100), "target"),
+    ("viewshed", 100, 100): (1.41e9 / 16384, "observer"),
+}
+ISSUE_SLOTS_PER_SM = 4  # one warp instruction per cycle from each SM sub-partition
+
 ROOFLINE_NOTES = {
-    "vix": "VIX is SM-issue bound, not HBM bound: its compulsory traffic is 3 B/cell and ncu shows "
-           "88.5% issue-active cycles, 3.54 warp instructions a cycle of 4 "
-           "(profiles/vix_kernel_c2_2048.md)",
+    "vix": "VIX is bound by SM instruction issue, not HBM: its compulsory traffic is 3 B/cell; "
+           "achieved = warp instructions per target (ncu) x targets / stage time, peak = SMs x "
+           "4 issue slots x the median SM clock of the timed region",
+    "viewshed": "VIEWSHED is bound by SM instruction issue (one dependent chain per ray); "
+                "achieved = warp instructions per observer (ncu) x observers / stage time",
     "site": "SITE's algorithmic bytes are the reference's rescoring traffic (every rescored "
             "candidate's shed and coverage window per pick); this kernel updates gains by "
-            "per-pick deltas and reads less (traffic), and is bound by the latency of its "
-            "dependent rounds (two group barriers each), not by HBM "
-            "(profiles/site_kernel_c2_2048.md)",
-    "viewshed": "VIEWSHED is SM-issue bound (one dependent chain per ray); its HBM traffic is "
-                "the shed output (profiles/shed_kernel2_c2_2048.md)",
+            "per-pick deltas and reads less (traffic); it is bound by the latency of its "
+            "dependent rounds, not by HBM",
 }
 
 
 def roofline(out, w, state, peaks, stage_ms_mean):
-    """Roofline of the dominant stage (largest mean device time)."""
+    """Roofline of the dominant stage (largest mean device time), and every
+    stage's HBM and (for VIX and VIEWSHED) issue-slot fractions."""
+    import torch
+
     dem, d_obs, d_sel, r, ctx, g = state
     hbm = peaks.get("hbm_gbs", 6800.0)
     src = "measured" if "hbm_gbs" in peaks else "fallback"
@@ -329,64 +347,307 @@ def roofline(out, w, state, peaks, stage_ms_mean):
     order = ctx.last_pick_order(g.nwanted)
     site_ref_bytes = site_algorithmic_bytes(w["nrows"], w["roi"], obs, order, g.nwanted)
     sb = stage_bytes(w, g.nwanted, site_ref_bytes)
+    traffic = NCU_TRAFFIC.get(out["config"]["workload"], {})
+    sms = torch.cuda.get_device_properties(torch.cuda.current_device()).multi_processor_count
+    mhz = out["clocks"].get("sm_mhz") or peaks.get("sm_max_mhz", 2070.0)
+    issue_peak = sms * ISSUE_SLOTS_PER_SM * mhz * 1e6  # warp instructions / s
+    units = {"vix": w["nrows"] ** 2 * w["ntests"], "viewshed": g.nwanted}
     stages = {}
     for k, ms in stage_ms_mean.items():
         ach = sb[k] / (ms / 1e3) / 1e9
-        stages[k] = {"ms": ms, "alg_bytes": sb[k], "achieved_gbs": ach, "frac": ach / hbm}
+        st = {"ms": ms, "alg_bytes": sb[k], "achieved_gbs": ach, "hbm_frac": ach / hbm}
+        if k in traffic:
+            st["dram_bytes"] = traffic[k]
+            st["dram_frac"] = traffic[k] / (ms / 1e3) / 1e9 / hbm
+        iw = ISSUE_WORK.get((k, w["roi"], w["ntests"]))
+        if iw:
+            per_unit, unit = iw
+            ips = per_unit * units[k] / (ms / 1e3)
+            st.update(issue_frac=ips / issue_peak, warp_instructions_per_s=ips,
+                      warp_instructions_per_unit=per_unit, unit_of_work=unit)
+        stages[k] = st
     dom = max(stage_ms_mean, key=stage_ms_mean.get)
     d = stages[dom]
-    traffic = NCU_TRAFFIC.get(out["config"]["workload"], {}).get(dom)
-    line = {"kernel": dom, "bound": "hbm", "achieved": d["achieved_gbs"], "peak": hbm,
-            "unit": "GB/s", "frac": d["frac"], "traffic": traffic,
-            "peak_source": f"{src} (MEASURED_PEAKS.json hbm_gbs)" if src == "measured" else
-            "fallback 6800 GB/s"}
+    hbm_part = {"achieved": d["achieved_gbs"], "peak": hbm, "unit": "GB/s", "frac": d["hbm_frac"],
+                "peak_source": f"{src} (hbm_gbs)" if src == "measured" else "fallback 6800 GB/s"}
+    if "issue_frac" in d:
+        line = {"kernel": dom, "bound": "sm_issue",
+                "achieved": d["warp_instructions_per_s"] / 1e12, "peak": issue_peak / 1e12,
+                "unit": "T warp-instructions/s", "frac": d["issue_frac"],
+                "traffic": traffic.get(dom),
+                "peak_source": f"{sms} SMs x {ISSUE_SLOTS_PER_SM} issue slots x {mhz:.0f} MHz "
+                               "(median SM clock of the timed region)",
+                "warp_instructions_per_unit": d["warp_instructions_per_unit"],
+                "unit_of_work": d["unit_of_work"], "hbm": hbm_part}
+    else:
+        line = {"kernel": dom, "bound": "hbm", "achieved": d["achieved_gbs"], "peak": hbm,
+                "unit": "GB/s", "frac": d["hbm_frac"], "traffic": traffic.get(dom),
+                "peak_source": hbm_part["peak_source"]}
+        if "dram_frac" in d:
+            line["dram_frac"] = d["dram_frac"]
     if dom in ROOFLINE_NOTES:
         line["note"] = ROOFLINE_NOTES[dom]
-    work = {"vix_targets": w["nrows"] ** 2 * w["ntests"],
-            "vix_targets_per_s": w["nrows"] ** 2 * w["ntests"] / (stage_ms_mean["vix"] / 1e3),
+    work = {"vix_targets": units["vix"],
+            "vix_targets_per_s": units["vix"] / (stage_ms_mean["vix"] / 1e3),
             "site_rounds": r.site_rounds, "site_picks": r.nusedsheds}
     return line, stages, work
 
 
-def run_reference(args, w):
-    """CPU implementation of the pipeline on a bounded sample of the workload."""
-    sys.path.insert(0, os.path.join(ROOT, "tests"))
-    from oracle_bind import Oracle, reference_available
+def fullsize_parity(workload, obs, sel, res):
+    """The job's outputs against the reference's own recorded outputs for
+    this workload (the full-size golden fixture, generated by seqsite), when
+    there is one: observers, selection, observer count and covered cells."""
+    import hashlib
 
-    kind = "reference_omp" if reference_available() and os.path.exists(
-        os.path.join(ROOT, "oracle", "_ref", "libsitingref_omp.so")) else "port"
-    orc = Oracle(kind if kind == "port" else "reference_omp")
-    if kind == "port":
-        orc.lib.oracle_set_threads(os.cpu_count() or 1)
-    rows = min(args.cpu_sample_rows, w["nrows"])
-    full = make_dem(w)
-    sample = full.reshape(w["nrows"], w["nrows"])[:rows, :rows].copy().ravel()
-    nw = max(1, int(w["nwanted0"] * (rows / w["nrows"]) ** 2))
-    times = []
-    # the reference's SITE prints its own progress line on stdout: keep it off
-    # the bench's single JSON line
-    sys.stdout.flush()
-    saved = os.dup(1)
-    os.dup2(2, 1)
+    with open(os.path.join(ROOT, "tests", "golden", "golden.json")) as f:
+        cases = {c["name"]: c for c in json.load(f).get("fullsize", [])}
+    c = cases.get(workload)
+    if c is None:
+        return None
+    sha = lambda a: hashlib.sha256(np.ascontiguousarray(a).tobytes()).hexdigest()  # noqa: E731
+    checks = {"observers": sha(obs) == c["obs_sha256"],
+              "selected": sha(sel) == c["selected_sha256"],
+              "nusedsheds": res.nusedsheds == c["nused"],
+              "cumarea": res.cumarea == c["cumarea"]}
+    return {"against": "reference seqsite outputs recorded in the full-size golden fixture",
+            "bit_exact": all(checks.values()), "checks": checks,
+            "selected_disagreeing": int(np.count_nonzero(sel)) - c["nused"]
+            if not checks["selected"] else 0}
+
+
+# cusite (siting.cu) rebuilt for sm_103a, as a reported comparison.  Its
+# FINDMAX kernel (siting.cu:164-224) starts thread t of a 256-thread CTA at
+# point t*ceil(npoints/256) of its block; where that is past the block's
+# points the thread reads other blocks' cells, and in the last block row
+# cells past the end of the VIX array.  It is run only where every block keeps
+# every thread inside the block, within its other fixed limits (a 500 000-entry
+# candidate list, siting.cu:645; nr threads a CTA, siting.cu:672).
+def cusite_runs_in_bounds(w, geo):
+    nr = 2 * w["roi"] + 1
+    if geo.nwanted > 499999 or nr > 1024:
+        return False
+    bs = np.float32(geo.blocksize)
+    n = w["nrows"]
+    edges = [min(int(bs * np.float32(b)), n) for b in range(geo.nblocks + 1)]
+    sizes = [b - a for a, b in zip(edges, edges[1:])]
+    for sx in set(sizes):
+        for sy in set(sizes):
+            npoints = sx * sy
+            per = -(-npoints // 256)
+            if 255 * per >= npoints:
+                return False
+    return True
+
+
+def cusite_column(w, dem, geo):
+    from oracle_bind import REF_CUSITE
+
+    if not os.path.exists(REF_CUSITE):
+        return {"skipped": "cusite not built here (the reference's siting.cu is not staged)"}
+    if not cusite_runs_in_bounds(w, geo):
+        return {"skipped": "with these parameters cusite's FINDMAX reads outside its blocks "
+                           "(past the VIX array in the last block row); not run"}
+    path = write_dem_file(dem)
     try:
-        for i in range(args.warmup + args.steps):
-            t0 = time.perf_counter()
-            orc.run(sample, rows, w["roi"], w["height"], w["ntests"], w["bw"], nw, w["intervis"])
-            dt = time.perf_counter() - t0
-            if i >= args.warmup:
-                times.append(dt)
+        r = time_reference_program(REF_CUSITE, w, path, "GPU")
     finally:
+        os.unlink(path)
+    r.pop("threads", None)
+    r.pop("cores", None)
+    r["build"] = "siting.cu with its makefile's command, -arch=sm_35 -> " \
+                 "-gencode arch=compute_103a,code=sm_103a"
+    r["note"] = "its results differ from seqsite (float division, FMA contraction, racy " \
+                "reductions), so it is a timing comparison only; its times include its own " \
+                "CUDA context creation, allocations and host copies"
+    return r
+
+
+def reference_inputs(w):
+    """The workload's DEM and block geometry from the CPU side alone (the
+    oracle's own generator, byte-equal to the library's, and the geometry of
+    siting.cpp:688-695): the reference arm never loads the library."""
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    from oracle_bind import Oracle
+
+    port = Oracle("port")
+    dem = port.fbm_dem(w["nrows"], w["seed"], octaves=w["octaves"],
+                       ridged_weight=w["ridged"], range_max=w["range_max"])
+    return dem, port.geometry(w["nrows"], w["bw"], w["nwanted0"])
+
+
+class _StdoutToStderr:
+    """The reference's SITE prints its progress line on stdout: keep it off
+    the bench's single JSON line."""
+
+    def __enter__(self):
+        sys.stdout.flush()
+        self.saved = os.dup(1)
+        os.dup2(2, 1)
+
+    def __exit__(self, *exc):
         import ctypes
 
-        ctypes.CDLL(None).fflush(None)  # the C library's buffered output goes to stderr too
-        os.dup2(saved, 1)
-        os.close(saved)
-    mean = sum(times) / len(times)
+        ctypes.CDLL(None).fflush(None)  # C and C++ buffered output goes to stderr too
+        os.dup2(self.saved, 1)
+        os.close(self.saved)
+
+
+def time_reference_library(w, dem, geo, warmup, steps, budget_s):
+    """The reference's own CPU code (siting.cpp built with OpenMP, library
+    form) on the whole workload with every host thread: each step runs the
+    four stages of main (siting.cpp:737-759) on the in-memory DEM, like the
+    GPU arm's device-resident step.  Without the reference's sources the
+    oracle port (same stages, deterministic) stands in and says so.  Steps
+    stop early once `budget_s` of CPU time is spent (at least one)."""
+    from oracle_bind import REF_OMP_SO, Oracle
+
+    n, roi = w["nrows"], w["roi"]
     cores = os.cpu_count() or 1
-    return {"kind": "reference" if kind != "port" else "port", "value": rows * rows / mean,
-            "unit": "cells/s", "cores": cores, "seconds_per_step": mean,
-            "sample": f"{rows}x{rows} corner of the {w['nrows']}^2 workload DEM, same parameters, "
-                      f"nwanted scaled to {nw}; whole pipeline"}
+    if os.path.exists(REF_OMP_SO):
+        orc, kind = Oracle("reference_omp"), "reference_omp"
+    else:
+        orc, kind = Oracle("port"), "port"
+    threads = orc.set_threads(cores)
+    nr = 2 * roi + 1
+    nwpr = (nr + 63) // 64
+    vix = np.empty(n * n, np.uint8)
+    obs = np.empty(geo.nwanted, np.int32)
+    sheds = np.empty(geo.nwanted * nr * nwpr, np.uint64)
+    sel = np.empty(geo.nwanted, np.uint8)
+    lib = orc.lib
+    h = w["height"]
+
+    def step():
+        t = [time.perf_counter()]
+        if kind == "port":
+            sheds.fill(0)  # the reference's calc_sheds zeroes its own output
+            lib.oracle_calc_vix(n, dem, roi, h, h, w["ntests"], vix)
+            t.append(time.perf_counter())
+            lib.oracle_find_max(n, vix, geo.blocksize, geo.nblocks, geo.nwantedperblock, obs)
+            t.append(time.perf_counter())
+            lib.oracle_calc_sheds(n, dem, roi, h, h, geo.nwanted, obs, sheds)
+            t.append(time.perf_counter())
+            cum = __import__("ctypes").c_longlong()
+            lib.oracle_site_it(n, roi, w["intervis"], geo.nwanted, obs, sheds, sel,
+                               __import__("ctypes").byref(cum), None)
+        else:
+            lib.ref_calc_vix(n, dem, roi, h, h, w["ntests"], vix)
+            t.append(time.perf_counter())
+            lib.ref_find_max(n, vix, geo.blocksize, geo.nwanted, geo.nblocks,
+                             geo.nwantedperblock, obs)
+            t.append(time.perf_counter())
+            lib.ref_calc_sheds(n, dem, roi, h, h, geo.nwanted, obs, sheds)
+            t.append(time.perf_counter())
+            lib.ref_site_it(n, roi, w["intervis"], geo.nwanted, obs, sheds, sel)
+        t.append(time.perf_counter())
+        return [b - a for a, b in zip(t, t[1:])]
+
+    spent, warm, runs = 0.0, 0, []
+    with _StdoutToStderr():
+        for i in range(warmup + steps):
+            st = step()
+            spent += sum(st)
+            if i < warmup:
+                warm += 1
+            else:
+                runs.append(st)
+            if spent >= budget_s and runs:
+                break
+            if i < warmup and spent >= budget_s / 2:  # no more warm-up than half the budget
+                warmup = i + 1
+    mean = sum(sum(r) for r in runs) / len(runs)
+    stages = {k: sum(r[j] for r in runs) / len(runs)
+              for j, k in enumerate(("vix", "findmax", "viewshed", "site"))}
+    return {"kind": kind, "value": n * n / mean, "unit": "cells/s", "cores": cores,
+            "threads": threads, "seconds_per_step": mean, "steps": len(runs), "warmup": warm,
+            "stages_s": stages, "nusedsheds": int(sel.sum()),
+            "sample": f"the whole {n}x{n} job (no sampling), DEM in host memory, "
+                      f"{len(runs)} timed run(s); "
+                      + ("the reference's siting.cpp compiled with OpenMP in library form, "
+                         f"omp_set_num_threads({threads})" if kind != "port" else
+                         "oracle port (reference sources not staged on this machine)")}
+
+
+_TIMING_KEYS = ("input", "vix", "findmax", "viewshed", "site", "output", "total")
+
+
+def _parse_timing_line(text):
+    """The reference programs' stdout line `input:.. vix:.. ... total:..`."""
+    import re
+
+    out = {}
+    for k, v in re.findall(r"([a-z]+):([-+0-9.eE]+)", text):
+        out[k] = float(v)
+    return out
+
+
+def time_reference_program(exe, w, dem_path, threads_note):
+    """One run of a reference program (ompsite as its makefile builds it, or
+    cusite rebuilt for sm_103a) through its own command line on the
+    workload's DEM file: its own stage-timing line, plus the wall clock."""
+    import tempfile
+
+    with tempfile.TemporaryDirectory() as td:
+        out = os.path.join(td, "observers.txt")
+        cmd = [exe, str(w["nrows"]), str(w["roi"]), str(w["height"]), str(w["ntests"]),
+               str(w["bw"]), str(w["nwanted0"]), str(w["intervis"]), dem_path, out]
+        t0 = time.perf_counter()
+        r = subprocess.run(cmd, capture_output=True, text=True, timeout=900)
+        wall = time.perf_counter() - t0
+        if r.returncode != 0:
+            return {"error": f"exit {r.returncode}: {(r.stdout + r.stderr).strip()[-200:]}"}
+        tl = _parse_timing_line(r.stdout)
+        nobs = sum(1 for _ in open(out))
+    total = tl.get("total", wall)
+    return {"value": w["nrows"] ** 2 / total, "unit": "cells/s", "seconds": total,
+            "wall_s": wall, "stages_s": {k: tl[k] for k in _TIMING_KEYS if k in tl},
+            "nusedsheds": int(tl.get("nusedsheds", nobs)), "coverage": tl.get("coverage"),
+            "observers": nobs, "threads": threads_note, "cores": os.cpu_count() or 1,
+            "command": " ".join([os.path.basename(exe)] + cmd[1:8] + ["dem.raw", "observers.txt"])}
+
+
+def write_dem_file(dem):
+    import tempfile
+
+    fd, path = tempfile.mkstemp(suffix=".raw")
+    with os.fdopen(fd, "wb") as f:
+        f.write(np.ascontiguousarray(dem, np.uint16).tobytes())
+    return path
+
+
+def run_reference_arm(args, w):
+    """`--impl reference`: the reference's own CPU implementation on the same
+    workload and parameters as the GPU arm, no library code on the path."""
+    dem, geo = reference_inputs(w)
+    cb = time_reference_library(w, dem, geo, warmup=min(args.warmup, 1), steps=args.steps,
+                                budget_s=args.reference_budget_s)
+    from oracle_bind import REF_OMPSITE
+
+    shipped = None
+    if os.path.exists(REF_OMPSITE):
+        path = write_dem_file(dem)
+        try:
+            shipped = time_reference_program(REF_OMPSITE, w, path,
+                                             "50 (hard-coded, siting.cpp:633-636)")
+        finally:
+            os.unlink(path)
+    config = workload_config(args, w, args.gpus, geo.nwanted)
+    line = {"metric": METRIC, "value": cb["value"], "unit": "cells/s", "n_gpus": args.gpus,
+            "steps": cb["steps"], "warmup": cb["warmup"], "steps_requested": args.steps,
+            "warmup_requested": args.warmup,
+            "ms_per_step": cb["seconds_per_step"] * 1e3, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32/u64", "data": "synthetic",
+            "config": config, "impl": "reference",
+            "cpu_baseline": {k: cb[k] for k in ("value", "unit", "cores", "threads", "kind",
+                                                "sample")},
+            "e2e": {"value": cb["value"], "unit": "cells/s", "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0},
+            "stages_s": cb["stages_s"], "nusedsheds": cb["nusedsheds"],
+            "note": f"each step is one whole job; steps stop after "
+                    f"{args.reference_budget_s:.0f} s of CPU time (at least one)"}
+    if shipped is not None:
+        line["ompsite_as_shipped"] = shipped
+    print(json.dumps(line))
 
 
 def run_batch_workload(args):
@@ -554,7 +815,8 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--workload", default="c2_4096",
                     choices=sorted(WORKLOADS) + ["c3_batch", "c5_serve"])
-    ap.add_argument("--cpu-sample-rows", type=int, default=2048)
+    ap.add_argument("--reference-budget-s", type=float, default=90.0,
+                    help="CPU seconds after which the reference arm stops timing more steps")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--batch-jobs", type=int, default=64)
     ap.add_argument("--autotune", action="store_true",
@@ -580,23 +842,8 @@ def main():
     w = WORKLOADS[args.workload]
 
     if args.impl == "reference":
-        if rank != 0:
-            return
-        import siting_gb300 as sg
-
-        cb = run_reference(args, w)
-        nwanted = sg.block_geometry(w["nrows"], w["bw"], w["nwanted0"]).nwanted
-        line = {"metric": METRIC, "value": cb["value"], "unit": "cells/s", "n_gpus": args.gpus,
-                "steps": args.steps, "warmup": args.warmup,
-                "ms_per_step": cb["seconds_per_step"] * 1e3, "higher_is_better": True,
-                "scaling": "weak", "vs_baseline": None, "dtype": "f32/u64", "data": "synthetic",
-                "config": dict(workload_config(args, w, args.gpus, nwanted),
-                               sample=cb["sample"]),
-                "impl": "reference",
-                "cpu_baseline": {k: cb[k] for k in ("value", "unit", "cores", "kind", "sample")},
-                "e2e": {"value": cb["value"], "unit": "cells/s", "h2d_bytes_per_step": 0,
-                        "d2h_bytes_per_step": 0}}
-        print(json.dumps(line))
+        if rank == 0:  # under torchrun the other ranks exit without work
+            run_reference_arm(args, w)
         return
 
     out, state, stage_ms = run_gpu(args, w)
@@ -611,10 +858,19 @@ def main():
     out["roofline"] = line
     out["roofline_stages"] = stages
     out["stage_work"] = work
+    par = fullsize_parity(args.workload, state[1].cpu().numpy(), state[2].cpu().numpy(), state[3])
+    if par is not None:
+        out["parity"] = par
     if not args.no_cpu_baseline and int(os.environ.get("WORLD_SIZE", "1")) == 1:
-        cb = run_reference(argparse.Namespace(warmup=0, steps=1,
-                                              cpu_sample_rows=args.cpu_sample_rows), w)
-        out["cpu_baseline"] = {k: cb[k] for k in ("value", "unit", "cores", "kind", "sample")}
+        # one whole job of the reference's OpenMP code on the host cores
+        sys.path.insert(0, os.path.join(ROOT, "tests"))
+        from oracle_bind import Oracle
+
+        geo = Oracle("port").geometry(w["nrows"], w["bw"], w["nwanted0"])
+        cb = time_reference_library(w, state[0], geo, warmup=0, steps=1, budget_s=0)
+        out["cpu_baseline"] = {k: cb[k] for k in ("value", "unit", "cores", "threads", "kind",
+                                                  "sample")}
+        out["cusite_baseline"] = cusite_column(w, state[0], geo)
     print(json.dumps(out))
 
 

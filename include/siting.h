@@ -176,10 +176,11 @@ int siting_last_site_phase_cycles(siting_ctx *ctx, long long *cycles, int n);
  * Scratch comes from a 16 MiB array in the library's device image, held by
  * every GPU that loads the library until the process exits; a job whose
  * scratch would exceed it returns SITING_ENOMEM, and invalid arguments return
- * SITING_EINVAL.  Runs on `stream` (a cudaStream_t, NULL = default stream) of
- * the current device and returns when the results are in `selected` and res.
- * The first call on a device looks up the array's device address; make that
- * first call before any stream capture.  All calls share the array: calls
+ * SITING_EINVAL (an observer index outside the DEM is found before SITE
+ * reads through it).  Runs on `stream` (a cudaStream_t, NULL = default
+ * stream) of the current device, synchronises that stream twice and returns
+ * when the results are in `selected` and res.  Each call looks up the array's
+ * device address on the current device.  All calls share the array: calls
  * that overlap on the GPU race and must be serialised by the caller. */
 int siting_site_it_noalloc(int nrows, int roi, int intervis, int nsheds,
                            const int32_t *d_obs, const uint64_t *d_sheds,

@@ -1,9 +1,9 @@
 // Library form of the reference's own CPU program (test infrastructure only).
 //
 // This translation unit is compiled by oracle/Makefile against the unmodified
-// reference source `siting.cpp` found on the include path; the source is never
-// copied into this repository.  `main` is renamed so that the four stage
-// functions can be called one at a time:
+// reference source `siting.cpp` found on the include path (the staged,
+// git-ignored copy under oracle/_ref/src; it is never committed).  `main` is
+// renamed so that the four stage functions can be called one at a time:
 //   calc_vix    siting.cpp:192-198
 //   find_max    siting.cpp:235-241
 //   calc_sheds  siting.cpp:349-360
@@ -60,5 +60,19 @@ void ref_site_it(int nrows, int roi, int intervis, int nsheds,
 }
 
 int ref_main(int argc, char **argv) { return siting_ref_main(argc, argv); }
+
+// Thread count of the OpenMP build's parallel loops (the program itself fixes
+// 50 threads in main, siting.cpp:633-636); returns the count in force, 1 for
+// the sequential build.
+int ref_set_threads(int n) {
+#ifdef _OPENMP
+  omp_set_dynamic(0);
+  if (n > 0) omp_set_num_threads(n);
+  return omp_get_max_threads();
+#else
+  (void)n;
+  return 1;
+#endif
+}
 
 }  // extern "C"

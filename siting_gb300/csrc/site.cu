@@ -40,7 +40,6 @@
 #include <algorithm>
 #include <cmath>
 #include <cstring>
-#include <mutex>
 #include <vector>
 
 #include "common.cuh"
@@ -1290,7 +1289,6 @@ cudaError_t launch_site(int nrows, int roi, int intervis, int nsheds, const int3
 namespace {
 
 constexpr size_t kNoAllocScratchBytes = size_t(16) << 20;  // 16 MiB per device
-constexpr int kMaxDevices = 64;
 
 }  // namespace
 
@@ -1298,22 +1296,18 @@ static __device__ __align__(256) unsigned char g_site_noalloc_scratch[kNoAllocSc
 
 namespace {
 
-std::mutex g_noalloc_mu;
-void *g_noalloc_base[kMaxDevices] = {};
-
-// Device address of the scratch array on the current device, looked up once
-// per device (host code only sees a host-side stand-in for the symbol).
-int noalloc_scratch(int dev, void **out) {
-  std::lock_guard<std::mutex> lock(g_noalloc_mu);
-  if (!g_noalloc_base[dev]) {
-    void *p = nullptr;
-    if (cudaGetSymbolAddress(&p, g_site_noalloc_scratch) != cudaSuccess || !p) {
-      cudaGetLastError();
-      return SITING_ECUDA;
-    }
-    g_noalloc_base[dev] = p;
+// Device address of the scratch array on the current device (host code only
+// sees a host-side stand-in for the symbol).  Looked up on every call, with
+// that device current, so that a context torn down and created again (for
+// example after cudaDeviceReset) never leaves a stale address behind; the
+// lookup costs microseconds against a SITE run.
+int noalloc_scratch(void **out) {
+  void *p = nullptr;
+  if (cudaGetSymbolAddress(&p, g_site_noalloc_scratch) != cudaSuccess || !p) {
+    cudaGetLastError();
+    return SITING_ECUDA;
   }
-  *out = g_noalloc_base[dev];
+  *out = p;
   return SITING_OK;
 }
 
@@ -1334,7 +1328,7 @@ extern "C" int siting_site_it_noalloc(int nrows, int roi, int intervis, int nshe
   }
   if (nsheds == 0) return SITING_OK;
   int dev = 0, sms = 0;
-  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) return SITING_EDEVICE;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0) return SITING_EDEVICE;
   if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
     return SITING_EDEVICE;
   const int G = site_default_ctas(nsheds, sms);
@@ -1345,7 +1339,7 @@ extern "C" int siting_site_it_noalloc(int nrows, int roi, int intervis, int nshe
   const size_t need = site_scratch_bytes(nrows, nsheds, G, roi) + 256;  // + error flag
   if (need > kNoAllocScratchBytes) return SITING_ENOMEM;  // beyond the 16 MiB array
   void *base = nullptr;
-  int rc = noalloc_scratch(dev, &base);
+  int rc = noalloc_scratch(&base);
   if (rc) return rc;
   cudaStream_t st = static_cast<cudaStream_t>(stream);
   SiteScratch s;
@@ -1356,12 +1350,19 @@ extern "C" int siting_site_it_noalloc(int nrows, int roi, int intervis, int nshe
       cudaMemsetAsync(d_err, 0, sizeof(int), st) != cudaSuccess ||
       cudaMemsetAsync(d_selected, 0, nsheds, st) != cudaSuccess)
     return SITING_ECUDA;
-  if (launch_check_obs(d_obs, nsheds, nrows, d_err, st) != cudaSuccess) return SITING_ECUDA;
+  // the observer indices are checked before SITE reads any cell through them:
+  // a bad index returns SITING_EINVAL with no SITE launch
+  int herr = 0;
+  if (launch_check_obs(d_obs, nsheds, nrows, d_err, st) != cudaSuccess ||
+      cudaMemcpyAsync(&herr, d_err, sizeof(int), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+      cudaStreamSynchronize(st) != cudaSuccess)
+    return SITING_ECUDA;
+  if (herr & kErrBadInput) return SITING_EINVAL;
+  if (herr) return SITING_ECUDA;
   if (launch_site(nrows, roi, intervis, nsheds, d_obs, d_sheds, bs, 1, nsheds, d_selected, s, G,
                   d_err, st) != cudaSuccess)
     return SITING_ECUDA;
   long long out[3] = {0, 0, 0};
-  int herr = 0;
   if (cudaMemcpyAsync(out, s.out, sizeof(out), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
       cudaMemcpyAsync(&herr, d_err, sizeof(int), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
       cudaStreamSynchronize(st) != cudaSuccess)

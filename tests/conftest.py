@@ -12,7 +12,6 @@ for p in (ROOT, TESTS):
         sys.path.insert(0, p)
 
 GOLDEN = os.path.join(TESTS, "golden", "golden.json")
-DEM_BIN_CANDIDATES = [os.path.join(ROOT, "oracle", "_ref", "dem.bin"), "/root/reference/dem.bin"]
 
 
 def pytest_configure(config):
@@ -53,10 +52,10 @@ def ctx(native):
 
 
 def dem_bin_path():
-    for p in DEM_BIN_CANDIDATES:
-        if os.path.exists(p):
-            return p
-    return None
+    """The reference's sample DEM, where its files are staged (oracle/_ref/src)."""
+    from oracle_bind import ref_dem_bin
+
+    return ref_dem_bin()
 
 
 def make_dem(spec, n):

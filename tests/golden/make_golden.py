@@ -12,6 +12,14 @@ recorded as sha256 digests (VIX bytes, observers, every viewshed word, the
 selection), with the observer count, the covered-cell count and the md5 of the
 observers file.  The reference's sample DEM (dem.bin) is recorded the same way
 when it is present.
+
+The full-size cases (key "fullsize": the 4096^2 workload, roi 100, 65 536
+observers, intervis 1) take minutes of sequential reference time each; they
+are (re)generated alone with
+
+    python tests/golden/make_golden.py --fullsize
+
+which keeps the small cases as they are.
 """
 from __future__ import annotations
 
@@ -27,7 +35,7 @@ ROOT = os.path.dirname(os.path.dirname(HERE))
 sys.path.insert(0, ROOT)
 sys.path.insert(0, os.path.dirname(HERE))
 
-from oracle_bind import Oracle, observers_text  # noqa: E402
+from oracle_bind import Oracle, observers_text, ref_dem_bin  # noqa: E402
 
 # (name, dem spec, nrows, roi, height, ntests, bw, nwanted0, intervis)
 CASES = [
@@ -44,7 +52,15 @@ CASES = [
     ("c1_fbm1000", {"seed": 11, "octaves": 8, "range_max": 10000}, 1000, 50, 100, 50, 10, 10000, 0),
 ]
 
-DEM_BIN = "/root/reference/dem.bin"
+
+
+# The full-size workloads: (name, dem spec, nrows, roi, height, ntests, bw,
+# nwanted0, intervis).  c2_4096 is the benchmark's headline job: 4096^2 fBm
+# with 10 octaves and ridged noise at weight 0.3, range 0-30000.
+FULLSIZE = [
+    ("c2_4096", {"seed": 4096, "octaves": 10, "ridged_weight": 0.3, "range_max": 30000},
+     4096, 100, 200, 100, 16, 65536, 1),
+]
 
 
 def make_dem(spec, n):
@@ -69,7 +85,7 @@ def record(orc: Oracle, dem, n, roi, h, ntests, bw, nw0, iv):
         "vix_sum": int(r["vix"].sum(dtype=np.int64)),
         "obs_sha256": sha(r["obs"]),
         "sheds_sha256": sha(r["sheds"]),
-        "shed_bits": int(np.unpackbits(r["sheds"].view(np.uint8)).sum()),
+        "shed_bits": int(np.bitwise_count(r["sheds"]).sum(dtype=np.int64)),
         "selected_sha256": sha(r["selected"]),
         "nused": int(r["nused"]),
         "cumarea": int(r["cumarea"]),
@@ -77,8 +93,26 @@ def record(orc: Oracle, dem, n, roi, h, ntests, bw, nw0, iv):
     }
 
 
+def fullsize(orc: Oracle):
+    path = os.path.join(HERE, "golden.json")
+    with open(path) as f:
+        out = json.load(f)
+    out["fullsize"] = []
+    for name, spec, n, roi, h, ntests, bw, nw0, iv in FULLSIZE:
+        dem = make_dem(spec, n)
+        rec = record(orc, dem, n, roi, h, ntests, bw, nw0, iv)
+        rec.update(name=name, dem=spec, args=[n, roi, h, ntests, bw, nw0, iv])
+        out["fullsize"].append(rec)
+        print(name, rec["nused"], rec["cumarea"], rec["observers_md5"], flush=True)
+    with open(path, "w") as f:
+        json.dump(out, f, indent=1)
+
+
 def main():
     orc = Oracle("reference")
+    if "--fullsize" in sys.argv:
+        fullsize(orc)
+        return
     out = {"generator": "reference siting.cpp built -DSEQ -ffp-contract=off (oracle/Makefile ref)",
            "cases": []}
     for name, spec, n, roi, h, ntests, bw, nw0, iv in CASES:
@@ -87,15 +121,19 @@ def main():
         rec.update(name=name, dem=spec, args=[n, roi, h, ntests, bw, nw0, iv])
         out["cases"].append(rec)
         print(name, rec["nused"], rec["cumarea"], flush=True)
-    if os.path.exists(DEM_BIN):
-        dem = np.fromfile(DEM_BIN, np.uint16)
+    if ref_dem_bin():
+        dem = np.fromfile(ref_dem_bin(), np.uint16)
         for iv in (0, 1):
             rec = record(orc, dem, 1000, 50, 100, 50, 10, 10000, iv)
             rec.update(name=f"dem_bin_iv{iv}", dem={"file": "dem.bin"},
                        args=[1000, 50, 100, 50, 10, 10000, iv])
             out["cases"].append(rec)
             print(rec["name"], rec["nused"], rec["cumarea"], rec["observers_md5"], flush=True)
-    with open(os.path.join(HERE, "golden.json"), "w") as f:
+    path = os.path.join(HERE, "golden.json")
+    if os.path.exists(path):
+        with open(path) as f:
+            out["fullsize"] = json.load(f).get("fullsize", [])
+    with open(path, "w") as f:
         json.dump(out, f, indent=1)
 
 

@@ -6,7 +6,10 @@ Two CPU implementations share one Python interface:
   semantics, OpenMP), built by ``oracle/Makefile`` on any machine.
 * ``Oracle("reference")``: the reference's own ``siting.cpp`` compiled with
   ``-DSEQ`` from its sources (``oracle/_ref/libsitingref.so``); present only
-  where those sources were available to build it.
+  where those sources were available to build it (a reference checkout, or
+  the git-ignored copy ``make -C oracle stage`` puts in ``oracle/_ref/src``).
+* ``Oracle("reference_omp")``: the same source built with OpenMP (ompsite in
+  library form), for timing only.
 
 Only tests, the smoke check and the bench's CPU-baseline leg use this module.
 """
@@ -23,8 +26,14 @@ import numpy as np
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 ORACLE_DIR = os.path.join(ROOT, "oracle")
 PORT_SO = os.path.join(ORACLE_DIR, "liboracle.so")
-REF_SO = os.path.join(ORACLE_DIR, "_ref", "libsitingref.so")
-REF_OMP_SO = os.path.join(ORACLE_DIR, "_ref", "libsitingref_omp.so")
+REF_DIR = os.path.join(ORACLE_DIR, "_ref")
+# the reference's own files, staged from a reference checkout by
+# `make -C oracle stage` (git-ignored; travels with the working tree)
+REF_SRC = os.environ.get("SITING_REFERENCE_SRC", os.path.join(REF_DIR, "src"))
+REF_SO = os.path.join(REF_DIR, "libsitingref.so")
+REF_OMP_SO = os.path.join(REF_DIR, "libsitingref_omp.so")
+REF_OMPSITE = os.path.join(REF_DIR, "ompsite")
+REF_CUSITE = os.path.join(REF_DIR, "cusite_sm103a")
 
 _lock = threading.Lock()
 _u16p = np.ctypeslib.ndpointer(np.uint16, flags="C_CONTIGUOUS")
@@ -42,6 +51,12 @@ def build_port() -> str:
 
 def reference_available() -> bool:
     return os.path.exists(REF_SO)
+
+
+def ref_dem_bin() -> str | None:
+    """The reference's sample DEM (dem.bin), if it is staged here."""
+    p = os.path.join(REF_SRC, "dem.bin")
+    return p if os.path.exists(p) else None
 
 
 def _load(path: str) -> C.CDLL:
@@ -87,6 +102,9 @@ class Oracle:
                                              C.c_void_p, C.c_int, _u8p]
             lib.oracle_threads.restype = C.c_int
             lib.oracle_set_threads.argtypes = [C.c_int]
+            lib.oracle_fbm_dem.argtypes = [_u16p, C.c_int, C.c_uint64, C.c_int, C.c_double,
+                                           C.c_double, C.c_double, C.c_double, C.c_int]
+            lib.oracle_fbm_dem.restype = C.c_int
         elif kind in ("reference", "reference_omp"):
             path = REF_SO if kind == "reference" else REF_OMP_SO
             if not os.path.exists(path):
@@ -99,9 +117,31 @@ class Oracle:
             lib.ref_calc_sheds.argtypes = [C.c_int, _u16p, C.c_int, C.c_int, C.c_int, C.c_int,
                                            _i32p, _u64p]
             lib.ref_site_it.argtypes = [C.c_int, C.c_int, C.c_int, C.c_int, _i32p, _u64p, _u8p]
+            lib.ref_set_threads.argtypes = [C.c_int]
+            lib.ref_set_threads.restype = C.c_int
         else:
             raise ValueError(kind)
         self.lib = lib
+
+    def set_threads(self, n: int) -> int:
+        """OpenMP threads of the parallel loops; returns the count in force."""
+        if self.kind == "port":
+            self.lib.oracle_set_threads(n)
+            return int(self.lib.oracle_threads())
+        return int(self.lib.ref_set_threads(n))
+
+    def fbm_dem(self, nrows: int, seed: int, octaves: int = 8, persistence: float = 0.5,
+                lacunarity: float = 2.0, base_wavelength: float = 256.0,
+                ridged_weight: float = 0.0, range_max: int = 10000) -> np.ndarray:
+        """Seeded fBm DEM (port only): the same bytes as the library's
+        generator for the same arguments, without loading the library."""
+        port = self if self.kind == "port" else Oracle("port")
+        out = np.empty(nrows * nrows, np.uint16)
+        rc = port.lib.oracle_fbm_dem(out, nrows, seed, octaves, persistence, lacunarity,
+                                     base_wavelength, ridged_weight, range_max)
+        if rc:
+            raise ValueError(f"oracle_fbm_dem: status {rc}")
+        return out
 
     # -- stages ------------------------------------------------------------
     def geometry(self, nrows: int, bw: int, nwanted0: int) -> Geometry:

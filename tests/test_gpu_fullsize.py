@@ -66,3 +66,56 @@ def test_c4_16384_stagewise(native, oracle, ctx):
     assert (res.nusedsheds, res.cumarea) == (nused, cumarea)
     assert oracle.union_count(N, ROI, obs, sheds, sel) == cumarea
     assert 100.0 * cumarea / (N * N) > 95.0
+
+
+def _bit_count(a):
+    """Set bits of an array (numpy >= 2 has a vectorised popcount)."""
+    if hasattr(np, "bitwise_count"):
+        return int(np.bitwise_count(a).sum(dtype=np.int64))
+    table = np.array([bin(i).count("1") for i in range(256)], np.int64)
+    return int(table[np.ascontiguousarray(a).view(np.uint8)].sum())
+
+
+def _fullsize_case(golden, name):
+    for c in golden.get("fullsize", []):
+        if c["name"] == name:
+            return c
+    pytest.skip(f"no full-size fixture {name}")
+
+
+def test_c2_4096_matches_reference_outputs(native, ctx, golden):
+    """The benchmark's headline job (4096^2 fBm + ridged noise, roi 100, 100
+    targets, bw 16, 65 536 observers, intervis 1) against the outputs the
+    reference's own seqsite recorded for it: every stage's bytes (VIX,
+    observers, every viewshed word, selection), the observer count, the
+    covered cells and the observers file (siting.cpp:501-626 at intervis 1,
+    where the multi-pick rounds and the intervis cut are stressed hardest)."""
+    import hashlib
+
+    c = _fullsize_case(golden, "c2_4096")
+    n, roi, h, ntests, bw, nw0, iv = c["args"]
+    spec = {k: v for k, v in c["dem"].items() if k != "seed"}
+    dem = native.fbm_dem(n, c["dem"]["seed"], **spec)
+    sha = lambda a: hashlib.sha256(np.ascontiguousarray(a).tobytes()).hexdigest()  # noqa: E731
+    assert sha(dem) == c["dem_sha256"], "input DEM differs from the fixture's"
+    g = native.block_geometry(n, bw, nw0)
+    assert g.nwanted == c["nwanted"]
+
+    vix = ctx.calc_vix(n, dem, roi, h, h, ntests)
+    assert int(vix.sum(dtype=np.int64)) == c["vix_sum"]
+    assert sha(vix) == c["vix_sha256"], "VIX differs from the reference's"
+    obs = ctx.find_max(n, vix.copy(), g.blocksize, g.nwanted, g.nblocks, g.nwantedperblock)
+    assert sha(obs) == c["obs_sha256"], "observers differ from the reference's"
+    sheds = ctx.calc_sheds(n, dem, roi, h, h, obs)
+    assert _bit_count(sheds) == c["shed_bits"]
+    assert sha(sheds) == c["sheds_sha256"], "viewsheds differ from the reference's"
+    sel, res = ctx.site_it(n, roi, iv, obs, sheds)
+    assert (res.nusedsheds, res.cumarea) == (c["nused"], c["cumarea"])
+    assert sha(sel) == c["selected_sha256"], "selection differs from the reference's"
+
+    # and the whole pipeline in one call, as the benchmark runs it
+    p = native.Params(nrows=n, roi=roi, height=h, ntests=ntests, bw=bw, nwanted0=nw0, intervis=iv)
+    obs2, sel2, res2 = ctx.run(p, dem)
+    assert sha(obs2) == c["obs_sha256"] and sha(sel2) == c["selected_sha256"]
+    assert (res2.nusedsheds, res2.cumarea) == (c["nused"], c["cumarea"])
+    assert hashlib.md5(native.observers_text(obs2, sel2, n)).hexdigest() == c["observers_md5"]

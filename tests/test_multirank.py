@@ -54,12 +54,33 @@ def test_reference_arm_under_torchrun(native):
     cmd = [sys.executable, "-m", "torch.distributed.run", "--nnodes=1", "--nproc-per-node", "2",
            "--master-addr", "127.0.0.1", "--master-port", str(_free_port()),
            os.path.join(ROOT, "bench.py"), "--impl", "reference", "--gpus", "2",
-           "--workload", "c1_1000", "--steps", "1", "--warmup", "0", "--cpu-sample-rows", "96"]
+           "--workload", "fbm_256", "--steps", "1", "--warmup", "0"]
     r = subprocess.run(cmd, cwd=ROOT, capture_output=True, text=True, timeout=300)
     assert r.returncode == 0, r.stderr[-2000:]
     lines = [json.loads(x) for x in r.stdout.splitlines() if x.startswith("{")]
     assert len(lines) == 1
     line = lines[0]
     assert line["impl"] == "reference" and line["value"] > 0
-    assert line["config"]["workload"] == "c1_1000" and line["config"]["nwanted"] == 10000
+    assert line["config"]["workload"] == "fbm_256" and line["config"]["nwanted"] == 256
     assert line["e2e"]["h2d_bytes_per_step"] == 0
+
+
+def test_reference_arm_never_loads_the_library():
+    """The reference arm builds its inputs with the oracle's generator and
+    times the reference's own code: the library (siting_gb300 and its .so)
+    stays unloaded in that process."""
+    code = (
+        "import runpy, sys\n"
+        "sys.argv = ['bench.py', '--impl', 'reference', '--workload', 'fbm_256',"
+        " '--steps', '1', '--warmup', '0']\n"
+        "runpy.run_path('bench.py', run_name='__main__')\n"
+        "maps = open('/proc/self/maps').read()\n"
+        "bad = [m for m in sys.modules if m.startswith('siting_gb300')]\n"
+        "print('LIBRARY', bool(bad) or 'libsiting_gb300' in maps)\n")
+    r = subprocess.run([sys.executable, "-c", code], cwd=ROOT, capture_output=True, text=True,
+                       timeout=300)
+    assert r.returncode == 0, r.stderr[-2000:]
+    line = json.loads(next(x for x in r.stdout.splitlines() if x.startswith("{")))
+    assert line["impl"] == "reference" and line["value"] > 0
+    assert line["cpu_baseline"]["kind"] in ("reference_omp", "port")
+    assert "LIBRARY False" in r.stdout

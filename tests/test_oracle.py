@@ -110,3 +110,27 @@ def test_reciprocal_identity_exhaustive():
     a = (1.0 / d).astype(np.float32)
     b = np.float32(1.0) / d.astype(np.float32)
     assert np.array_equal(a, b)
+
+
+def test_oracle_matches_reference_golden_c2_4096(oracle, native, golden):
+    """The oracle at the benchmark's full 4096^2 size (65 536 observers,
+    intervis 1) against the outputs the reference's seqsite recorded."""
+    cases = {c["name"]: c for c in golden.get("fullsize", [])}
+    if "c2_4096" not in cases:
+        pytest.skip("no full-size fixture")
+    test_oracle_matches_reference_golden(cases["c2_4096"], oracle, native)
+
+
+# The workloads' DEM recipes: (nrows, seed, octaves, ridged weight, range).
+DEM_RECIPES = [(1000, 1000, 8, 0.0, 10000), (4096, 4096, 10, 0.3, 30000),
+               (16384, 16384, 12, 0.0, 40000)]
+
+
+@pytest.mark.parametrize("n,seed,octaves,ridged,rmax", DEM_RECIPES,
+                         ids=["c1_1000", "c2_4096", "c4_16384"])
+def test_oracle_dem_generator_equals_library(oracle, native, n, seed, octaves, ridged, rmax):
+    """The CPU baseline builds its inputs with the oracle's own generator, so
+    that it never loads the library: both must give the same bytes."""
+    a = oracle.fbm_dem(n, seed, octaves=octaves, ridged_weight=ridged, range_max=rmax)
+    b = native.fbm_dem(n, seed, octaves=octaves, ridged_weight=ridged, range_max=rmax)
+    assert np.array_equal(a, b)

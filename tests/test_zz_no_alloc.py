@@ -64,3 +64,20 @@ def test_noalloc_rejects_jobs_beyond_its_scratch(native):
     rc = native.load().siting_site_it_noalloc(20000, 10, 0, 1, d.data_ptr(), d.data_ptr(),
                                               d.data_ptr(), None, C.byref(res))
     assert rc == 2  # SITING_ENOMEM
+
+
+def test_noalloc_flags_bad_observer_indices_before_site(native):
+    torch = pytest.importorskip("torch")
+    # one index past the DEM and one negative: the index check runs before
+    # SITE and the call returns SITING_EINVAL without reading through them
+    n, roi = 64, 5
+    nr = 2 * roi + 1
+    obs = torch.tensor([0, n * n + 5, 7, -3], dtype=torch.int32, device="cuda")
+    sheds = torch.zeros(len(obs) * nr, dtype=torch.int64, device="cuda")
+    sel = torch.full((len(obs),), 7, dtype=torch.uint8, device="cuda")
+    res = native._ResultC()
+    rc = native.load().siting_site_it_noalloc(n, roi, 0, len(obs), obs.data_ptr(),
+                                              sheds.data_ptr(), sel.data_ptr(), None,
+                                              C.byref(res))
+    assert rc == 1  # SITING_EINVAL
+    assert res.nusedsheds == 0 and int(sel.sum().item()) == 0
