@@ -695,6 +695,8 @@ def run_batch_workload(args):
         all(torch.equal(a, b) for a, b in zip(sel_b, sel_p)) and \
         all((x.nusedsheds, x.cumarea) == (y.nusedsheds, y.cumarea) for x, y in zip(rb, rp))
     mb, mp = sum(tb) / len(tb), sum(tp) / len(tp)
+    cb.close()
+    cp.close()
     out = {"metric": METRIC + " (batched)", "value": cells / (mb / 1e3), "unit": "cells/s",
            "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": mb,
            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32/u64",
@@ -707,7 +709,7 @@ def run_batch_workload(args):
                               "vix_findmax_viewshed": rb[0].ms_vix,
                               "site_after_them": rb[0].ms_site},
            "site_rounds_max": max(r.site_rounds for r in rb)}
-    print(json.dumps(out))
+    return out
 
 
 # The serving workload: a Poisson stream of requests, sides log-uniform in
@@ -804,7 +806,7 @@ def run_serve_workload(args):
            "gpu_busy_frac": st["busy_s"] / max(span, 1e-9),
            "peak_workspace_gb": st["peak_workspace"] / (1 << 30),
            "checked_alone": min(args.serve_check, len(served)), "bit_identical_alone": same}
-    print(json.dumps(out))
+    return out
 
 
 def main():
@@ -818,12 +820,14 @@ def main():
     ap.add_argument("--reference-budget-s", type=float, default=90.0,
                     help="CPU seconds after which the reference arm stops timing more steps")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-extras", action="store_true",
+                    help="headline job only: no batched or serving measurements")
     ap.add_argument("--batch-jobs", type=int, default=64)
     ap.add_argument("--autotune", action="store_true",
                     help="time the launch plans on a corner of the DEM first (siting_autotune)")
     ap.add_argument("--autotune-rows", type=int, default=1024)
     ap.add_argument("--serve-requests", type=int, default=2000)
-    ap.add_argument("--serve-rate", type=float, default=50.0, help="mean arrivals per second")
+    ap.add_argument("--serve-rate", type=float, default=100.0, help="mean arrivals per second")
     ap.add_argument("--serve-budget-gb", type=float, default=150.0)
     ap.add_argument("--serve-check", type=int, default=8,
                     help="requests re-run alone and compared bit for bit")
@@ -833,11 +837,11 @@ def main():
     rank = int(os.environ.get("RANK", "0"))
     if args.workload == "c5_serve":
         if args.impl == "gb300" and rank == 0:
-            run_serve_workload(args)
+            print(json.dumps(run_serve_workload(args)))
         return
     if args.workload == "c3_batch":
         if args.impl == "gb300" and rank == 0:
-            run_batch_workload(args)
+            print(json.dumps(run_batch_workload(args)))
         return
     w = WORKLOADS[args.workload]
 
@@ -871,6 +875,27 @@ def main():
         out["cpu_baseline"] = {k: cb[k] for k in ("value", "unit", "cores", "threads", "kind",
                                                   "sample")}
         out["cusite_baseline"] = cusite_column(w, state[0], geo)
+    if args.workload == "c2_4096" and not args.no_extras and \
+            int(os.environ.get("WORLD_SIZE", "1")) == 1:
+        # the batched and serving forms, measured in the same run (after the
+        # headline's timed region, with their own timing)
+        ctx = state[4]
+        del state
+        ctx.close()
+        import torch
+
+        torch.cuda.empty_cache()
+        b = run_batch_workload(argparse.Namespace(**{**vars(args), "steps": min(args.steps, 5),
+                                                     "warmup": min(args.warmup, 3)}))
+        out["batched"] = {k: b[k] for k in ("value", "unit", "ms_per_step", "steps", "warmup",
+                                             "plain", "speedup_vs_plain",
+                                             "bit_identical_to_plain", "batch_phase_ms",
+                                             "config")}
+        sv = run_serve_workload(args)
+        out["serving"] = {k: sv[k] for k in ("value", "unit", "latency_ms", "served", "refused",
+                                             "requests_per_s", "gpu_busy_frac", "config",
+                                             "checked_alone", "bit_identical_alone")
+                          if k in sv}
     print(json.dumps(out))
 
 
