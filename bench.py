@@ -733,19 +733,22 @@ def serve_jobs(nreq, seed=5):
     return jobs
 
 
-def run_serve_workload(args):
-    """Serving loop under a Poisson arrival stream: latency percentiles and
-    throughput; the first requests are re-run alone and compared."""
+def serve_rasters():
+    import siting_gb300 as sg
+
+    return [sg.fbm_dem(4096, 4096 * 7 + i, octaves=10, ridged_weight=0.3 * (i % 2),
+                       range_max=int(2000 + 5600 * i)).reshape(4096, 4096) for i in range(6)]
+
+
+def serve_at_rate(args, jobs, rasters, rate, seed=11):
+    """One Poisson arrival stream through a fresh server: per-request latency
+    (submission to results in host memory), throughput, admissions."""
     import queue
-    import threading
 
     import siting_gb300 as sg
 
-    jobs = serve_jobs(args.serve_requests)
-    rasters = [sg.fbm_dem(4096, 4096 * 7 + i, octaves=10, ridged_weight=0.3 * (i % 2),
-                          range_max=int(2000 + 5600 * i)).reshape(4096, 4096) for i in range(6)]
-    rng = np.random.default_rng(11)
-    gaps = rng.exponential(1.0 / args.serve_rate, size=len(jobs))
+    rng = np.random.default_rng(seed)
+    gaps = rng.exponential(1.0 / rate, size=len(jobs))
     budget = int(args.serve_budget_gb * (1 << 30))
     srv = sg.Server(0, hbm_budget=budget, max_batch_jobs=args.batch_jobs, reserve=True)
     # warm-up: a few requests before the clock starts
@@ -762,11 +765,13 @@ def run_serve_workload(args):
     th.start()
     t0 = time.perf_counter()
     due = t0
+    arrivals = []
     for (p, src, x0, y0), gap in zip(jobs, gaps):
         due += gap
         dt = due - time.perf_counter()
         if dt > 0:
             time.sleep(dt)
+        arrivals.append(due - t0)
         try:
             t = srv.submit(p, rasters[src][x0:x0 + p.nrows, y0:y0 + p.nrows])
         except sg.SitingError:
@@ -783,29 +788,94 @@ def run_serve_workload(args):
     lat = np.array([i.latency_s for _, i in served]) * 1e3
     cells = sum(t.params.nrows ** 2 for t, _ in served)
     span = max(i.t_done for _, i in served) - min(i.t_submit for _, i in served)
-    # bit-identity: the first requests alone through a plain context
+    return {"rate_per_s": rate, "requests": len(jobs), "value": cells / span, "unit": "cells/s",
+            "latency_ms": {"p50": float(np.percentile(lat, 50)),
+                           "p90": float(np.percentile(lat, 90)),
+                           "p99": float(np.percentile(lat, 99)), "max": float(lat.max())},
+            "served": len(served), "refused": refused, "wall_s": wall,
+            "requests_per_s": len(served) / span,
+            "admissions": st["batches"],
+            "mean_in_flight_at_admission": float(np.mean([i.batch_jobs for _, i in served])),
+            "gpu_busy_frac": st["busy_s"] / max(span, 1e-9),
+            "peak_workspace_gb": st["peak_workspace"] / (1 << 30),
+            "_served": served, "_arrivals": np.array(arrivals)}
+
+
+def plain_service_times(jobs, rasters, check=None):
+    """The plain loop: each request alone through siting_run (host buffers,
+    upload and readback included), one after another.  Returns the service
+    time of each, and whether the listed served requests' outputs equal it."""
+    import siting_gb300 as sg
+
     ctx = sg.Context(0)
-    same = True
-    for t, _ in served[:args.serve_check]:
-        o, s_, _r = ctx.run(t.params, np.ascontiguousarray(t.dem).ravel())
-        same &= bool(np.array_equal(o, t.obs) and np.array_equal(s_, t.selected))
+    times, same = [], True
+    check = check or {}
+    for i, (p, src, x0, y0) in enumerate(jobs):
+        dem = np.ascontiguousarray(rasters[src][x0:x0 + p.nrows, y0:y0 + p.nrows]).ravel()
+        t0 = time.perf_counter()
+        o, s_, _r = ctx.run(p, dem)
+        times.append(time.perf_counter() - t0)
+        if i in check:
+            t = check[i]
+            same &= bool(np.array_equal(o, t.obs) and np.array_equal(s_, t.selected))
     ctx.close()
-    out = {"metric": "DEM cells/s served", "value": cells / span, "unit": "cells/s",
-           "n_gpus": 1, "steps": len(served), "warmup": 3, "ms_per_step": span * 1e3 / len(served),
+    return np.array(times), same
+
+
+def fifo_latencies_ms(arrivals, service):
+    """Latency of each request in a one-at-a-time FIFO loop with these
+    arrivals (s) and service times (s)."""
+    done, out = 0.0, []
+    for a, sv in zip(arrivals, service):
+        done = max(done, a) + sv
+        out.append(done - a)
+    return np.array(out) * 1e3
+
+
+def run_serve_workload(args):
+    """Serving loop under a Poisson arrival stream: latency percentiles and
+    throughput against the plain one-request-at-a-time loop (the same
+    requests run alone one after another: its throughput, and its latencies
+    under the same arrivals from the measured service times); served
+    requests are compared with their solo runs bit for bit."""
+    rasters = serve_rasters()
+    rates = args.serve_sweep or [args.serve_rate]
+    per_rate = []
+    for rate in rates:
+        n = args.serve_requests if not args.serve_sweep else \
+            min(args.serve_requests, max(200, int(rate * 30)))
+        jobs = serve_jobs(n)
+        r = serve_at_rate(args, jobs, rasters, rate)
+        served = r.pop("_served")
+        arrivals = r.pop("_arrivals")
+        # the plain loop on the same requests (a prefix of them outside a sweep)
+        k = len(jobs) if args.serve_sweep else min(len(jobs), args.serve_plain)
+        check = {i: served[i][0] for i in range(min(args.serve_check, len(served)))}
+        svc, same = plain_service_times(jobs[:k], rasters, check)
+        cells_k = sum(p.nrows ** 2 for p, *_ in jobs[:k])
+        plain = {"value": cells_k / svc.sum(), "unit": "cells/s", "requests_timed": k}
+        if k == len(jobs):
+            fl = fifo_latencies_ms(arrivals, svc)
+            plain["latency_ms"] = {"p50": float(np.percentile(fl, 50)),
+                                   "p99": float(np.percentile(fl, 99))}
+        r["plain_loop"] = plain
+        r["speedup_vs_plain"] = r["value"] / plain["value"]
+        r["checked_alone"] = len(check)
+        r["bit_identical_alone"] = same
+        per_rate.append(r)
+    head = per_rate[0] if len(per_rate) == 1 else max(per_rate, key=lambda x: x["value"])
+    out = {"metric": "DEM cells/s served", "value": head["value"], "unit": "cells/s",
+           "n_gpus": 1, "steps": head["served"], "warmup": 3,
+           "ms_per_step": 1e3 / head["requests_per_s"],
            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32/u64",
            "data": "synthetic",
-           "config": {"workload": "serve_poisson", "requests": len(jobs),
-                      "rate_per_s": args.serve_rate, "hbm_budget_gb": args.serve_budget_gb,
-                      "max_batch_jobs": args.batch_jobs,
-                      "sides": "log-U[256,4096]", "roi": "U[20,200]", "nwanted": "n^2/128"},
-           "latency_ms": {"p50": float(np.percentile(lat, 50)), "p90": float(np.percentile(lat, 90)),
-                          "p99": float(np.percentile(lat, 99)), "max": float(lat.max())},
-           "served": len(served), "refused": refused, "wall_s": wall,
-           "requests_per_s": len(served) / span,
-           "batches": st["batches"], "mean_batch_jobs": len(served) / max(1, st["batches"]),
-           "gpu_busy_frac": st["busy_s"] / max(span, 1e-9),
-           "peak_workspace_gb": st["peak_workspace"] / (1 << 30),
-           "checked_alone": min(args.serve_check, len(served)), "bit_identical_alone": same}
+           "config": {"workload": "serve_poisson", "rate_per_s": head["rate_per_s"],
+                      "requests": head["requests"], "hbm_budget_gb": args.serve_budget_gb,
+                      "max_in_flight": args.batch_jobs, "sides": "log-U[256,4096]",
+                      "roi": "U[20,200]", "nwanted": "n^2/128"}}
+    out.update({k: v for k, v in head.items() if k not in ("value", "unit")})
+    if len(per_rate) > 1:
+        out["sweep"] = per_rate
     return out
 
 
@@ -831,6 +901,10 @@ def main():
     ap.add_argument("--serve-budget-gb", type=float, default=150.0)
     ap.add_argument("--serve-check", type=int, default=8,
                     help="requests re-run alone and compared bit for bit")
+    ap.add_argument("--serve-plain", type=int, default=300,
+                    help="requests timed through the plain one-at-a-time loop (no sweep)")
+    ap.add_argument("--serve-sweep", type=float, nargs="*", default=None,
+                    help="arrival rates to sweep (requests: min(serve-requests, 30 s worth))")
     ap.add_argument("--site-ctas", type=int, default=0,
                     help="CTAs of the SITE kernel (0 = library default)")
     args = ap.parse_args()
@@ -894,7 +968,9 @@ def main():
         sv = run_serve_workload(args)
         out["serving"] = {k: sv[k] for k in ("value", "unit", "latency_ms", "served", "refused",
                                              "requests_per_s", "gpu_busy_frac", "config",
-                                             "checked_alone", "bit_identical_alone")
+                                             "mean_in_flight_at_admission", "plain_loop",
+                                             "speedup_vs_plain", "checked_alone",
+                                             "bit_identical_alone")
                           if k in sv}
     print(json.dumps(out))
 

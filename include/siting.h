@@ -250,31 +250,38 @@ int siting_autotune_clear(siting_ctx *ctx);
 
 /* ---- serving loop --------------------------------------------------------
  * No counterpart in the reference (one process per DEM there).  A server
- * owns a context and a worker thread: submitted jobs queue in arrival order;
- * whenever the GPU is free the worker takes the longest FIFO prefix of the
- * queue (at most max_batch_jobs) whose batch workspace fits the HBM budget
- * and runs it as one siting_run_batch (continuous batching).  A job that
- * alone exceeds the budget is refused at submission (SITING_ENOMEM).  The
- * workspace stays allocated between batches; with reserve != 0 the whole
- * budget is allocated at creation, so the serving path never allocates.
- * Each job's results equal siting_run's on the same input. */
+ * owns a context, a device arena of hbm_budget bytes (allocated at creation)
+ * and a worker thread, and keeps up to max_batch_jobs jobs in flight at once:
+ * the head of the arrival queue is admitted as soon as its workspace fits in
+ * the free part of the arena, while other jobs are on the GPU, and its
+ * kernels overlap theirs: its stages run on stage streams whose priority
+ * rises as jobs get smaller, its selection on the highest-priority stream as
+ * soon as its stages are done, so selections run in the order their stages
+ * finish.  A job that alone exceeds the budget is refused at submission
+ * (SITING_ENOMEM).  The serving path never allocates device memory.  Each
+ * job's results equal siting_run's on the same input. */
 typedef struct siting_server siting_server;
 
 typedef struct {
-  int status;                 /* SITING_OK or the batch's error */
-  siting_result result;       /* phase times are the batch's */
-  double t_submit, t_start, t_done; /* seconds since the server started */
-  int batch_id, batch_jobs;   /* which batch ran the job, and its size */
+  int status;                 /* SITING_OK or the job's error */
+  siting_result result;       /* counts only: no phase times */
+  double t_submit, t_start, t_done; /* seconds since the server started;
+                                       t_start: admitted to the GPU */
+  int batch_id, batch_jobs;   /* the admission that started the job, and the
+                                 jobs in flight right after it */
   char error[160];            /* message when status != SITING_OK */
 } siting_job_info;
 
 typedef struct {
   long long submitted, completed, refused, batches, pending;
-  size_t peak_workspace;      /* largest batch workspace run, bytes */
-  double busy_s;              /* time spent running batches */
+                              /* batches: admissions of one or more jobs */
+  size_t peak_workspace;      /* most arena bytes in use at once */
+  double busy_s;              /* time with at least one job in flight */
 } siting_server_stats;
 
-/* hbm_budget in bytes (required); max_batch_jobs <= 0 means 64. */
+/* hbm_budget in bytes (required); max_batch_jobs (jobs in flight at once)
+ * <= 0 means 64; reserve is accepted for compatibility (the arena is always
+ * allocated at creation). */
 int siting_server_create(int device, size_t hbm_budget, int max_batch_jobs,
                          int reserve, siting_server **out);
 /* Drains the queue, stops the worker and frees the context. */

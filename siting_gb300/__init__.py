@@ -490,7 +490,8 @@ class Ticket:
 
 
 class Server:
-    """Serving loop: continuous batching of submitted jobs under an HBM budget
+    """Serving loop: submitted jobs are admitted to the GPU while others are
+    in flight, as memory and slots free up, under an HBM budget
     (siting_server_* in the library; one worker thread owns the GPU)."""
 
     def __init__(self, device: int = 0, hbm_budget: int = 8 << 30, max_batch_jobs: int = 64,

@@ -91,3 +91,34 @@ def test_wait_unknown_ticket_and_timeout(native):
             srv.wait(t2, timeout=0.0)
         except TimeoutError:  # still queued or running: the ticket stays valid
             srv.wait(t2, timeout=120)
+
+
+def test_request_admitted_mid_flight_overlaps_and_matches_solo(ctx, native):
+    """Continuous admission: a small request submitted while a large job is on
+    the GPU starts before that job ends, finishes before it (its stages and
+    selection overlap the large job's on the device) and gives the same
+    result as a solo run."""
+    import time
+
+    big = native.Params(nrows=4096, roi=150, height=100, ntests=100, bw=16, nwanted0=65536,
+                        intervis=1)
+    small = native.Params(nrows=256, roi=20, height=30, ntests=32, bw=16, nwanted0=512,
+                          intervis=1)
+    big_dem = native.fbm_dem(4096, 41, octaves=10, range_max=20000)
+    small_dem = native.fbm_dem(256, 42, octaves=7, range_max=5000)
+    with native.Server(0, hbm_budget=16 << 30) as srv:
+        srv.wait(srv.submit(small, small_dem), timeout=300)  # warm: modules loaded
+        tb = srv.submit(big, big_dem)
+        time.sleep(0.005)  # the large job's stages are on the GPU by now
+        ts = srv.submit(small, small_dem)
+        obs_s, sel_s, info_s = srv.wait(ts, timeout=300)
+        obs_b, sel_b, info_b = srv.wait(tb, timeout=300)
+    assert info_s.status == native.OK and info_b.status == native.OK
+    assert info_s.t_start < info_b.t_done, "admitted only after the large job ended"
+    assert info_s.t_done < info_b.t_done, "did not overlap the large job"
+    assert info_s.batch_jobs >= 2  # two jobs in flight at its admission
+    o1, s1, r1 = ctx.run(small, small_dem)
+    assert np.array_equal(obs_s, o1) and np.array_equal(sel_s, s1)
+    assert (info_s.result.nusedsheds, info_s.result.cumarea) == (r1.nusedsheds, r1.cumarea)
+    o2, s2, r2 = ctx.run(big, big_dem)
+    assert np.array_equal(obs_b, o2) and np.array_equal(sel_b, s2)
