@@ -708,7 +708,15 @@ def run_batch_workload(args):
            "batch_phase_ms": {"upload": rb[0].ms_h2d,
                               "vix_findmax_viewshed": rb[0].ms_vix,
                               "site_after_them": rb[0].ms_site},
-           "site_rounds_max": max(r.site_rounds for r in rb)}
+           "site_rounds_max": max(r.site_rounds for r in rb),
+           # where the floor is: each job's stage times when it runs alone
+           # (the plain runs); VIX, FINDMAX and VIEWSHED already fill the GPU
+           # one job at a time, so their sum bounds any batching from below
+           "plain_stage_ms_sum": {k: float(sum(getattr(r, "ms_" + k) for r in rp))
+                                  for k in ("vix", "findmax", "viewshed", "site")}}
+    st_sum = out["plain_stage_ms_sum"]
+    out["floor_ms"] = st_sum["vix"] + st_sum["findmax"] + st_sum["viewshed"]
+    out["speedup_bound_vs_plain"] = mp / out["floor_ms"]
     return out
 
 
@@ -964,7 +972,8 @@ def main():
         out["batched"] = {k: b[k] for k in ("value", "unit", "ms_per_step", "steps", "warmup",
                                              "plain", "speedup_vs_plain",
                                              "bit_identical_to_plain", "batch_phase_ms",
-                                             "config")}
+                                             "plain_stage_ms_sum", "floor_ms",
+                                             "speedup_bound_vs_plain", "config")}
         sv = run_serve_workload(args)
         out["serving"] = {k: sv[k] for k in ("value", "unit", "latency_ms", "served", "refused",
                                              "requests_per_s", "gpu_busy_frac", "config",

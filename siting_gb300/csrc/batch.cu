@@ -30,6 +30,8 @@ int batch_site_ctas(int nsheds, int sm_count) {
   return std::min(std::min(g, std::max(1, nsheds)), sm_count);
 }
 
+constexpr int kBatchWaveCtas = 64;
+
 bool site_fits(const Job &J, int G) {
   return site_smem_bytes(J.p.roi, J.g.nwanted, G, J.g.nblocks, J.g.nwantedperblock,
                          J.g.blocksize) <= 220 * 1024;
@@ -81,13 +83,17 @@ int plan_batch(int sm_count, int njobs, const siting_params *params, const sitin
     if (jobs[a].p.intervis != jobs[b].p.intervis) return jobs[a].p.intervis > jobs[b].p.intervis;
     return jobs[a].G > jobs[b].G;
   });
+  // A SITE CTA fills its SM's register file, so a launch holds its SMs
+  // alone: waves take at most kBatchWaveCtas SMs, leaving the rest to the
+  // later jobs' stages that the waves overlap.
+  const int wave_cap = std::min(sm_count, kBatchWaveCtas);
   std::vector<std::vector<int>> &waves = bp->waves;
   std::vector<int> &wave_ctas = bp->wave_ctas;
   waves.clear();
   wave_ctas.clear();
   for (int j : order) {
     size_t w = 0;
-    while (w < waves.size() && wave_ctas[w] + jobs[j].G > sm_count) w++;
+    while (w < waves.size() && wave_ctas[w] + jobs[j].G > std::max(wave_cap, jobs[j].G)) w++;
     if (w == waves.size()) {
       waves.emplace_back();
       wave_ctas.push_back(0);
@@ -99,7 +105,7 @@ int plan_batch(int sm_count, int njobs, const siting_params *params, const sitin
   // its automatically planned groups in proportion to their candidates (a
   // group's rounds shorten with more CTAs), up to the single-job default
   for (size_t w = 0; w < waves.size(); w++) {
-    const int spare = sm_count - wave_ctas[w];
+    const int spare = wave_cap - wave_ctas[w];
     double total = 0;
     for (int j : waves[w])
       if (jobs[j].auto_G) total += jobs[j].g.nwanted;
