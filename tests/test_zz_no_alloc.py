@@ -5,8 +5,9 @@ their call path, such as a serving loop that reserves its whole HBM budget at
 start-up, or an application whose memory pool (PyTorch's caching allocator,
 for instance) already owns the GPU's memory.  It takes its scratch from a
 fixed array in the library's device image instead.  Its results must equal
-those of siting_site_it_dev, which allocates its workspace, bit for bit; two
-calls in a row check that the shared array is reset between calls.
+those of siting_site_it_dev, which allocates its workspace, bit for bit (and
+both the CPU oracle's selection); two calls in a row check that the shared
+array is reset between calls.
 
 This file is collected last so that a stop-at-first-failure run has already
 run every other test before it.
@@ -25,6 +26,12 @@ def _case(native, oracle, n, roi, h, ntests, bw, nw0, seed):
     return want["obs"], want["sheds"]
 
 
+def _oracle_selection(oracle, n, roi, iv, obs, sheds):
+    """The CPU oracle's SITE on the same candidates (seqsite semantics)."""
+    sel, nused, cumarea = oracle.site(n, roi, iv, obs, sheds)[:3]
+    return sel, nused, cumarea
+
+
 @pytest.mark.parametrize("iv", [0, 1])
 def test_noalloc_site_matches_allocating_entry(native, oracle, iv):
     torch = pytest.importorskip("torch")
@@ -41,6 +48,9 @@ def test_noalloc_site_matches_allocating_entry(native, oracle, iv):
         ctx.sync()
     sel_ref = d_sel_ref.cpu().numpy()
     assert ref.nusedsheds == int(sel_ref.sum()) > 0
+    # and both against the CPU oracle
+    sel_o, nused_o, cum_o = _oracle_selection(oracle, n, roi, iv, obs, sheds)
+    assert np.array_equal(sel_ref, sel_o) and (ref.nusedsheds, ref.cumarea) == (nused_o, cum_o)
 
     lib = native.load()
     stream = C.c_void_p(torch.cuda.current_stream().cuda_stream)
