@@ -74,6 +74,7 @@ cudaError_t launch_sheds(const DemView &dem, int roi, int oht, int tht, int nshe
 struct SiteScratch {
   uint64_t *cum;             // nrows * ceil(nrows/64) words, zeroed before launch
   uint64_t *nbits;           // the round's new bits of each pick: [64][nr][nwpr+1] words
+  unsigned char *nmask;      // [64][nr]: bit j set when word j of that new-bit row is nonzero
   unsigned long long *topk;  // [2][nctas][top-K] x {key, cell}: published top keys
   int *cuts;                 // [2][nctas]: per-CTA prefix cut (intervis)
   int *ncount;               // [2][64]: popcount of each pick's new bits (self-check)

@@ -64,6 +64,7 @@ constexpr int kTopK = 3;
 constexpr int kMaxPicks = 64;    // picks accepted in one round at most
 constexpr int kSmallRecip = 128; // reciprocals tabled in shared memory (>= kMaxPicks)
 constexpr int kMaxPairs = 8192;  // (candidate, pick) pairs one CTA updates per round
+constexpr int kMaskCap = 8192;   // shared bytes for a spread round's new-bit word masks
 
 struct SiteArgs {
   int n, roi, intervis, nsheds, G;
@@ -73,6 +74,7 @@ struct SiteArgs {
   int nb, npb;
   uint64_t *cum0;   // coverage bitmap, updated in place
   uint64_t *nbits;  // [kMaxPicks][nr][nwpr+1]: the round's new bits of each pick
+  unsigned char *nmask;  // [kMaxPicks][nr]: bit j set when word j of that row is nonzero
   int ncap_words;   // shared-memory words for a small round's new bits
   unsigned long long *topk;  // [2][G][kTopK] x {key, cell}
   int *cuts;                 // [2][G]: per-CTA cut of the round's prefix (intervis)
@@ -228,6 +230,7 @@ __global__ void __launch_bounds__(kThreads, 1)
   unsigned char *s_tag = take((size_t)a.nslots);  // bit0 touched, bit1 covered (this round)
   unsigned char *s_dirty = take((size_t)ngroups);
   uint64_t *s_N = reinterpret_cast<uint64_t *>(take((size_t)a.ncap_words * 8));
+  unsigned char *s_nmask = take(kMaskCap);
 
   GroupBarrier gb{a.bar, (unsigned)G, 0u};
   // tracing: device cycles per phase, accumulated by CTA 0's thread 0 in
@@ -489,6 +492,7 @@ __global__ void __launch_bounds__(kThreads, 1)
             const int W = fwp + q;
             x[q] = (row_in && q < nb2 && W >= 0 && W < cw) ? __ldcg(xr + W) : ~0ull;
           }
+          unsigned msk = 0;
 #pragma unroll
           for (int q = 0; q < 8; q++) {
             if (q >= nb2) break;
@@ -497,7 +501,9 @@ __global__ void __launch_bounds__(kThreads, 1)
             __stcg(nrow + q, v);
             if (own_n) s_N[(size_t)i * nb2 + q] = v;
             cnt += __popcll(v);
+            msk |= (v != 0ull) << q;
           }
+          __stcg(a.nmask + pi * nr + prow, (unsigned char)msk);
         } else {
           for (int j = 0; j < nb2; j++) {
             const int W = fwp + j;
@@ -665,6 +671,22 @@ __global__ void __launch_bounds__(kThreads, 1)
     // every CTA's rows of N are written
     if (!group_sync(gb, a.err, &s_flagv)) return;
     mark(11);
+    // the rows' nonzero-word masks into shared memory (a few hundred bytes):
+    // an item whose candidate's columns meet only zero words of the pick's
+    // new bits loads nothing (a third of the items at 4096²)
+    const bool masked = nwpr <= 7 && m * nr <= kMaskCap;
+    if (masked) {
+      const int n16 = (m * nr + 15) / 16;
+      const uint4 *src = reinterpret_cast<const uint4 *>(a.nmask);
+      for (int i = tid; i < n16; i += blockDim.x)
+        reinterpret_cast<uint4 *>(s_nmask)[i] = __ldcg(src + i);
+      __syncthreads();
+    }
+    // bits j of the N words an item reads: columns lo..hi of the row
+    auto need = [&](int pi, int prow, int lo, int hi, int fwp) -> unsigned {
+      const unsigned span = ((1u << (hi - lo + 1)) - 1u) << (lo - fwp);
+      return masked ? span & s_nmask[pi * nr + prow] : span;
+    };
     if (kThreads == 512 && nwpr <= 4) {
       // ---- D2 for narrow sheds: two (pair, row) items a thread in flight
       // (512-thread CTAs only: the 1024-thread build has no registers for it).
@@ -686,21 +708,26 @@ __global__ void __launch_bounds__(kThreads, 1)
         shed_align(cy - roi, fwc, fbc);
         shed_align(py - roi, fwp, fbp);
         const uint64_t *nrow = a.nbits + (size_t)(pi * nr + prow) * nb2;
+        const unsigned rowm = masked ? s_nmask[pi * nr + prow] : 0xffu;
         if (a.intervis && r == roi) {  // own cell: newly covered by the pick?
           const int j = (cy >> 6) - fwp;
-          if (j >= 0 && j < nb2 && ((__ldcg(nrow + j) >> (63 - (cy & 63))) & 1ull))
+          if (j >= 0 && j < nb2 && ((rowm >> j) & 1u) &&
+              ((__ldcg(nrow + j) >> (63 - (cy & 63))) & 1ull))
             atomicOr(reinterpret_cast<unsigned *>(s_paircov + (pq & ~3)), 1u << (8 * (pq & 3)));
         }
         const int lo = max(max(fwc, fwp), 0);
         const int hi = min(min((cy + roi) >> 6, fwp + nwpr), cw - 1);
         if (lo > hi) return;
+        const unsigned nm = need(pi, prow, lo, hi, fwp);
+        if (!nm) return;  // the pick adds nothing under c's columns of this row
         const uint64_t *crow = a.sheds + (size_t)(s * G + k) * per + (size_t)r * nwpr;
 #pragma unroll
         for (int q = 0; q < 4; q++) w[q] = q < nwpr ? __ldg(crow + q) : 0ull;
 #pragma unroll
         for (int q = 0; q < 5; q++) {
           const int W = fwc + q;  // c's placed word q lands at column word fwc+q
-          x[q] = (q < nb2 && W >= lo && W <= hi) ? __ldcg(nrow + (W - fwp)) : 0ull;
+          x[q] = (q < nb2 && W >= lo && W <= hi && ((nm >> (W - fwp)) & 1u))
+                     ? __ldcg(nrow + (W - fwp)) : 0ull;
         }
         pr = pq;
       };
@@ -737,21 +764,26 @@ __global__ void __launch_bounds__(kThreads, 1)
         shed_align(cy - roi, fwc, fbc);
         shed_align(py - roi, fwp, fbp);
         const uint64_t *nrow = a.nbits + (size_t)(pi * nr + prow) * nb2;
+        const unsigned rowm = masked ? s_nmask[pi * nr + prow] : 0xffu;
         if (a.intervis && r == roi) {  // own cell: newly covered by the pick?
           const int j = (cy >> 6) - fwp;
-          if (j >= 0 && j < nb2 && ((__ldcg(nrow + j) >> (63 - (cy & 63))) & 1ull))
+          if (j >= 0 && j < nb2 && ((rowm >> j) & 1u) &&
+              ((__ldcg(nrow + j) >> (63 - (cy & 63))) & 1ull))
             atomicOr(reinterpret_cast<unsigned *>(s_paircov + (pr & ~3)), 1u << (8 * (pr & 3)));
         }
         const int lo = max(max(fwc, fwp), 0);
         const int hi = min(min((cy + roi) >> 6, fwp + nwpr), cw - 1);
         if (lo > hi) continue;
+        const unsigned nm = need(pi, prow, lo, hi, fwp);
+        if (!nm) continue;  // the pick adds nothing under c's columns of this row
         const uint64_t *crow = a.sheds + (size_t)(s * G + k) * per + (size_t)r * nwpr;
         uint64_t w[8], x[8];
 #pragma unroll
         for (int q = 0; q < 8; q++) {
           w[q] = q < nwpr ? __ldg(crow + q) : 0ull;
           const int W = fwc + q;  // c's placed word q lands at column word fwc+q
-          x[q] = (q < nb2 && W >= lo && W <= hi) ? __ldcg(nrow + (W - fwp)) : 0ull;
+          x[q] = (q < nb2 && W >= lo && W <= hi && ((nm >> (W - fwp)) & 1u))
+                     ? __ldcg(nrow + (W - fwp)) : 0ull;
         }
         int d = 0;
 #pragma unroll
@@ -1037,10 +1069,12 @@ size_t scratch_layout(int nrows, int nsheds, int nctas, int roi, unsigned char *
   unsigned char *gn = take((size_t)nsheds * 4);
   const size_t nr = 2 * (size_t)roi + 1;  // every row is written before it is read
   unsigned char *nb = take((size_t)kMaxPicks * nr * ((nr + 63) / 64 + 1) * 8);
+  unsigned char *nm = take((size_t)kMaxPicks * nr + 16);  // + the 16-byte loads' tail
   unsigned char *tb = take(site_job_table_bytes(1, nctas));
   if (s) {
     s->cum = reinterpret_cast<uint64_t *>(c0);
     s->nbits = reinterpret_cast<uint64_t *>(nb);
+    s->nmask = nm;
     s->topk = reinterpret_cast<unsigned long long *>(tk);
     s->cuts = reinterpret_cast<int *>(cu);
     s->ncount = reinterpret_cast<int *>(nc);
@@ -1139,6 +1173,7 @@ size_t site_smem_base(int roi, int nsheds, int nctas, int nblocks, int npb, floa
   b += 3 * round16((size_t)GK * 4) + round16((size_t)GK * 8) + 3 * round16(kMaxPicks * 4);
   b += 3 * round16((size_t)pair_cap * 4) + round16((size_t)pair_cap);
   b += 2 * round16((size_t)nslots) + round16((size_t)ngroups);
+  b += kMaskCap;
   return b;
 }
 
@@ -1180,6 +1215,7 @@ SiteArgs make_site_args(const SiteJob &j, int block0) {
   a.npb = j.npb;
   a.cum0 = j.scratch.cum;
   a.nbits = j.scratch.nbits;
+  a.nmask = j.scratch.nmask;
   a.ncap_words =
       site_ncap_words(site_smem_base(j.roi, j.nsheds, j.nctas, j.nblocks, j.npb, j.blocksize));
   a.topk = j.scratch.topk;
