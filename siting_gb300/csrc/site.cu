@@ -652,18 +652,26 @@ __global__ void __launch_bounds__(kThreads, 1)
         const int lo = max(max(fwc, fwp), 0);
         const int hi = min(min((cy + roi) >> 6, fwp + nwpr), cw - 1);
         if (lo > hi) continue;
+        // the pick's new bits under c's columns (shared memory) first: where
+        // they are all zero the item loads nothing from c's shed
+        uint64_t x[8], any = 0ull;
+#pragma unroll
+        for (int q = 0; q < 8; q++) {
+          const int W = fwc + q;  // c's placed word q lands at column word fwc+q
+          x[q] = (q < nb2 && W >= lo && W <= hi) ? nrow[W - fwp] : 0ull;
+          any |= x[q];
+        }
+        if (!any) continue;
         const uint64_t *crow = a.sheds + (size_t)(s * G + k) * per + (size_t)r * nwpr;
         uint64_t w[8];
 #pragma unroll
         for (int q = 0; q < 8; q++) w[q] = q < nwpr ? __ldg(crow + q) : 0ull;
         int d = 0;
 #pragma unroll
-        for (int q = 0; q < 8; q++) {  // c's placed word q lands at column word fwc+q
+        for (int q = 0; q < 8; q++) {
           if (q >= nb2) break;
-          const int W = fwc + q;
-          if (W < lo || W > hi) continue;
           const uint64_t vc = (w[q] >> fbc) | ((q > 0 && fbc) ? w[q - 1] << (64 - fbc) : 0ull);
-          d += __popcll(vc & nrow[W - fwp]);
+          d += __popcll(vc & x[q]);
         }
         if (d) atomicAdd(&s_pairdelta[pr], d);
       }
