@@ -695,6 +695,21 @@ def run_batch_workload(args):
         all(torch.equal(a, b) for a, b in zip(sel_b, sel_p)) and \
         all((x.nusedsheds, x.cumarea) == (y.nusedsheds, y.cumarea) for x, y in zip(rb, rp))
     mb, mp = sum(tb) / len(tb), sum(tp) / len(tp)
+    graph_stats = cb.batch_graph_stats()
+    # the launch forms of the batch's VIX and FINDMAX (siting_ctx_set_batch_mode:
+    # 1 = grids over many jobs' items, 2 = one launch per job), captured as a
+    # CUDA graph and replayed, or launched directly
+    forms = {}
+    for name, mode, graphs in (("merged_grids_graph", 1, True), ("per_job_graph", 2, True),
+                               ("per_job_direct", 2, False), ("merged_grids_direct", 1, False)):
+        cb.set_batch_mode(mode)
+        cb.set_batch_graphs(graphs)
+        for _ in range(2):
+            timed(sb, batched)
+        ts = [timed(sb, batched)[0] for _ in range(3)]
+        forms[name] = sum(ts) / len(ts)
+    cb.set_batch_mode(0)
+    cb.set_batch_graphs(True)
     cb.close()
     cp.close()
     out = {"metric": METRIC + " (batched)", "value": cells / (mb / 1e3), "unit": "cells/s",
@@ -709,6 +724,8 @@ def run_batch_workload(args):
                               "vix_findmax_viewshed": rb[0].ms_vix,
                               "site_after_them": rb[0].ms_site},
            "site_rounds_max": max(r.site_rounds for r in rb),
+           "graph": {"captures": graph_stats[0], "replays": graph_stats[1]},
+           "launch_forms_ms": forms,
            # where the floor is: each job's stage times when it runs alone
            # (the plain runs); VIX, FINDMAX and VIEWSHED already fill the GPU
            # one job at a time, so their sum bounds any batching from below

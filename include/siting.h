@@ -114,6 +114,22 @@ int siting_ctx_trim(siting_ctx *ctx);
 /* Tuning knob: CTAs of the SITE kernel (0 = automatic, capped at the SM
  * count).  Results do not depend on it. */
 int siting_ctx_set_site_ctas(siting_ctx *ctx, int nctas);
+/* Tuning knob of the batched form (no counterpart in the reference): how a
+ * batch launches VIX and FINDMAX.  1 = for the jobs of each SITE launch, one
+ * grid over their (job, tile) VIX items (two when some halos are staged and
+ * some not) and one over their (job, block) FINDMAX items, 2 = one VIX and
+ * one FINDMAX launch per job, 0 = automatic: 1 for the SITE launches whose
+ * jobs average at most 2^20 cells, else 2.  Results do not depend on it. */
+int siting_ctx_set_batch_mode(siting_ctx *ctx, int mode);
+/* Device-resident batches (siting_run_batch_dev) run as CUDA graphs (no
+ * counterpart in the reference): the first call of a batch captures its
+ * copies and launches, a later call with the same jobs, buffers and
+ * workspace replays the graph (on = 1, the default); 0 launches every call
+ * directly.  Results do not depend on it. */
+int siting_ctx_set_batch_graphs(siting_ctx *ctx, int on);
+/* Graphs captured and replayed by the context's batches so far. */
+int siting_ctx_batch_graph_stats(const siting_ctx *ctx, long long *captures,
+                                 long long *replays);
 /* Page-locked host memory for fast copies (cudaMallocHost / cudaFreeHost). */
 int siting_pinned_alloc(size_t bytes, void **out);
 int siting_pinned_free(void *p);
@@ -200,10 +216,13 @@ int siting_run_dev(siting_ctx *ctx, const siting_params *p,
 
 /* ---- batched form --------------------------------------------------------
  * Runs `njobs` independent jobs (DEMs of any sizes and parameters) as one
- * batch: every job's VIX, FINDMAX and VIEWSHED kernels are enqueued back to
- * back on the context's stream, then the greedy SITE selections of many jobs
- * run concurrently in shared cooperative launches (each job's CTA group with
- * its own barrier and scratch).  elevs[j] is job j's row-major uint16 DEM on
+ * batch: the jobs' VIX, FINDMAX and VIEWSHED kernels are enqueued on the
+ * context's stream (VIX and FINDMAX of small jobs as grids over many jobs'
+ * items, see siting_ctx_set_batch_mode), and the greedy SITE selections of
+ * many jobs run concurrently in shared cooperative launches (each job's CTA
+ * group with its own barrier and scratch) on a second stream, overlapping the
+ * later jobs' stages.  The device-resident form runs as a CUDA graph
+ * (siting_ctx_set_batch_graphs).  elevs[j] is job j's row-major uint16 DEM on
  * the host; obs[j] and selected[j] receive nwanted entries.  plans may be
  * NULL.  Each job's results equal siting_run's on the same input.  The
  * phase times in results are the batch's: ms_vix covers VIX, FINDMAX and

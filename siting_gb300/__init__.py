@@ -157,6 +157,9 @@ def load() -> C.CDLL:
         "siting_ctx_workspace_bytes": ([_P], sz),
         "siting_ctx_trim": ([_P], i),
         "siting_ctx_set_site_ctas": ([_P, i], i),
+        "siting_ctx_set_batch_mode": ([_P, i], i),
+        "siting_ctx_set_batch_graphs": ([_P, i], i),
+        "siting_ctx_batch_graph_stats": ([_P, C.POINTER(ll), C.POINTER(ll)], i),
         "siting_pinned_alloc": ([sz, C.POINTER(_P)], i),
         "siting_pinned_free": ([_P], i),
         "siting_calc_vix": ([_P, i, _P, i, i, i, i, _P], i),
@@ -312,6 +315,21 @@ class Context:
 
     def set_site_ctas(self, n: int):
         self._check(self._lib.siting_ctx_set_site_ctas(self.h, n))
+
+    def set_batch_mode(self, mode: int):
+        """How batches run VIX and FINDMAX: 0 automatic, 1 one queued launch per
+        SITE launch (FINDMAX fused), 2 one launch per stage and job."""
+        self._check(self._lib.siting_ctx_set_batch_mode(self.h, mode))
+
+    def set_batch_graphs(self, on: bool):
+        """Device-resident batches captured and replayed as CUDA graphs (default on)."""
+        self._check(self._lib.siting_ctx_set_batch_graphs(self.h, int(bool(on))))
+
+    def batch_graph_stats(self) -> tuple[int, int]:
+        """(graphs captured, graphs replayed) by this context's batches."""
+        c, r = C.c_longlong(), C.c_longlong()
+        self._check(self._lib.siting_ctx_batch_graph_stats(self.h, C.byref(c), C.byref(r)))
+        return c.value, r.value
 
     # ---- stages on host arrays (reference signatures) -----------------------
     def calc_vix(self, nrows, elevs, roi, oht, tht, ntests) -> np.ndarray:

@@ -12,6 +12,7 @@
 #include <string>
 #include <vector>
 
+#include "batch.h"
 #include "ctx.h"
 #include "kernels.h"
 #include "siting.h"
@@ -375,6 +376,7 @@ int siting_ctx_create(int device, size_t hbm_budget, siting_ctx **out) {
 int siting_ctx_trim(siting_ctx *ctx) {
   if (!ctx) return SITING_EINVAL;
   cudaStreamSynchronize(ctx->stream);
+  siting::batch_graph_reset(ctx);  // it refers to the workspace
   for (auto &b : ctx->buf) {
     if (b.p) cudaFree(b.p);
     b = DevBuf{};
@@ -392,6 +394,8 @@ int siting_ctx_destroy(siting_ctx *ctx) {
   for (auto &ev : ctx->ev)
     if (ev) cudaEventDestroy(ev);
   for (auto &ev : ctx->wave_ev) cudaEventDestroy(ev);
+  siting::batch_graph_reset(ctx);
+  if (ctx->bg_stage) cudaFreeHost(ctx->bg_stage);
   if (ctx->stream2) cudaStreamDestroy(ctx->stream2);
   if (ctx->stream) cudaStreamDestroy(ctx->stream);
   if (ctx->h_out) cudaFreeHost(ctx->h_out);
@@ -413,6 +417,26 @@ size_t siting_ctx_workspace_bytes(const siting_ctx *ctx) { return ctx ? ctx->hel
 int siting_ctx_set_site_ctas(siting_ctx *ctx, int nctas) {
   if (!ctx || nctas < 0) return SITING_EINVAL;
   ctx->site_ctas = nctas;
+  return SITING_OK;
+}
+
+int siting_ctx_set_batch_mode(siting_ctx *ctx, int mode) {
+  if (!ctx || mode < siting::kBatchAuto || mode > siting::kBatchPerJob) return SITING_EINVAL;
+  ctx->batch_mode = mode;
+  return SITING_OK;
+}
+
+int siting_ctx_set_batch_graphs(siting_ctx *ctx, int on) {
+  if (!ctx || (on != 0 && on != 1)) return SITING_EINVAL;
+  ctx->batch_graphs = on != 0;
+  if (!on) siting::batch_graph_reset(ctx);
+  return SITING_OK;
+}
+
+int siting_ctx_batch_graph_stats(const siting_ctx *ctx, long long *captures, long long *replays) {
+  if (!ctx) return SITING_EINVAL;
+  if (captures) *captures = ctx->bg_captures;
+  if (replays) *replays = ctx->bg_replays;
   return SITING_OK;
 }
 

@@ -157,6 +157,12 @@ int plan_batch(int sm_count, int njobs, const siting_params *params, const sitin
   return SITING_OK;
 }
 
+void batch_graph_reset(siting_ctx *ctx) {
+  if (ctx->bg_exec) cudaGraphExecDestroy(ctx->bg_exec);
+  ctx->bg_exec = nullptr;
+  ctx->bg_key.clear();
+}
+
 int run_batch(siting_ctx *ctx, int njobs, const siting_params *params,
               const uint16_t *const *elevs, const int *src_pitch, bool host_io,
               int32_t *const *obs_out, uint8_t *const *sel_out, siting_result *results,
@@ -198,11 +204,69 @@ int run_batch(siting_ctx *ctx, int njobs, const siting_params *params,
   const size_t s_tabs = 0, s_wtabs = align256(tab_bytes);
   const size_t s_out = s_wtabs + align256(wtab_bytes);
   const size_t s_bytes = s_out + (size_t)njobs * 16 * sizeof(long long);
-  unsigned char *stage;
-  if ((rc = stage_get(ctx, s_bytes, &stage))) return rc;
   cudaStream_t st = ctx->stream;
+  // the SITE stream has the highest priority: a cooperative SITE launch needs
+  // all its SMs at once, and the block scheduler then gives it SMs as stage
+  // CTAs end instead of refilling them from the stage grids
+  if (!ctx->stream2) {
+    int least = 0, greatest = 0;
+    CK(cudaDeviceGetStreamPriorityRange(&least, &greatest));
+    CK(cudaStreamCreateWithPriority(&ctx->stream2, cudaStreamNonBlocking, greatest));
+  }
+  while (ctx->wave_ev.size() < waves.size()) {
+    cudaEvent_t e;
+    CK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+    ctx->wave_ev.push_back(e);
+  }
+  cudaStream_t st2 = ctx->stream2;
 
-  CK(cudaEventRecord(ctx->ev[5], st));
+  // The device-resident form runs as a CUDA graph: the first call of a batch
+  // captures its copies and launches, and a later call with the same jobs,
+  // buffers and workspace replays the graph.  The graph's host staging is
+  // its own pinned buffer, so nothing else overwrites what a replay copies.
+  const bool graph = !host_io && ctx->batch_graphs;
+  std::vector<unsigned char> key;
+  if (graph) {
+    auto put = [&](const void *p, size_t n) {
+      const unsigned char *c = static_cast<const unsigned char *>(p);
+      key.insert(key.end(), c, c + n);
+    };
+    put(&njobs, sizeof(njobs));
+    put(params, sizeof(siting_params) * njobs);
+    put(elevs, sizeof(void *) * njobs);
+    put(obs_out, sizeof(void *) * njobs);
+    put(sel_out, sizeof(void *) * njobs);
+    for (int j = 0; j < njobs; j++) {
+      const int sp = src_pitch ? src_pitch[j] : 0;
+      put(&sp, sizeof(sp));
+      const siting_plan pl = plans ? plans[j] : siting_plan{0, -1, -1, 0};
+      put(&pl, sizeof(pl));
+    }
+    put(&base, sizeof(base));
+    put(&ctx->batch_mode, sizeof(ctx->batch_mode));
+  }
+  unsigned char *stage;
+  if (graph) {
+    if (ctx->bg_stage_cap < s_bytes) {
+      batch_graph_reset(ctx);
+      if (ctx->bg_stage) cudaFreeHost(ctx->bg_stage);
+      ctx->bg_stage = nullptr;
+      ctx->bg_stage_cap = 0;
+      CK(cudaMallocHost(&ctx->bg_stage, s_bytes));
+      ctx->bg_stage_cap = s_bytes;
+    }
+    stage = ctx->bg_stage;
+  } else if ((rc = stage_get(ctx, s_bytes, &stage))) {
+    return rc;
+  }
+
+  // Inside a capture, timing events are recorded as external events, so that
+  // the graph records them when it runs (a plain record inside a capture only
+  // orders the graph's nodes; outside one the flag is refused); the wave
+  // events and the join order work across streams.
+  auto enqueue = [&](bool capturing) -> int {
+  const unsigned rec_flags = capturing ? cudaEventRecordExternal : cudaEventRecordDefault;
+  CK(cudaEventRecordWithFlags(ctx->ev[5], st, rec_flags));
   for (int j = 0; j < njobs; j++) {  // inputs, VIX tables, zeroed scratch
     Job &J = jobs[j];
     const size_t sp = (size_t)(src_pitch && src_pitch[j] ? src_pitch[j] : J.n) * 2;
@@ -216,8 +280,9 @@ int run_batch(siting_ctx *ctx, int njobs, const siting_params *params,
     CK(cudaMemsetAsync(base + J.o_site, 0, J.site_zero, st));
     CK(cudaMemsetAsync(base + J.o_err, 0, 256, st));
   }
+
   CK(cudaMemcpyAsync(base + o_tabs, stage + s_tabs, tab_bytes, cudaMemcpyHostToDevice, st));
-  CK(cudaEventRecord(ctx->ev[0], st));
+  CK(cudaEventRecordWithFlags(ctx->ev[0], st, rec_flags));
   auto dem_of = [&](int j) {
     const Job &J = jobs[j];
     const bool own = host_io || J.n % 8 || (uintptr_t)elevs[j] % 16 ||
@@ -236,27 +301,51 @@ int run_batch(siting_ctx *ctx, int njobs, const siting_params *params,
   // soon as its jobs' viewsheds exist, overlapping the later jobs' stages.
   // (SITE launches wait for their peers at group barriers; the kernels they
   // share the SMs with never wait for SITE, so the barriers always complete.)
-  if (!ctx->stream2) CK(cudaStreamCreateWithFlags(&ctx->stream2, cudaStreamNonBlocking));
-  while (ctx->wave_ev.size() < waves.size()) {
-    cudaEvent_t e;
-    CK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
-    ctx->wave_ev.push_back(e);
-  }
-  cudaStream_t st2 = ctx->stream2;
+  std::vector<StageJob> qjobs;
   for (size_t w = 0; w < waves.size(); w++) {
+    // VIX and FINDMAX of the wave's jobs: one grid over their (job, tile)
+    // items (two when some halos are staged and some not) and one over their
+    // (job, block) items, or one launch per stage and job
+    qjobs.clear();
     for (int j : waves[w]) {
       const Job &J = jobs[j];
-      int *err = reinterpret_cast<int *>(base + J.o_err);
-      CK(launch_vix(dem_of(j), J.p.roi, J.p.oht, J.p.tht, J.p.ntests, base + J.o_vix,
-                    base + o_tabs + J.o_tab, J.vp, err, st));
-      CK(launch_findmax(base + J.o_vix, J.n, J.g.blocksize, J.g.nblocks, J.g.nwantedperblock,
-                        obs_of(j), st));
+      qjobs.push_back(StageJob{dem_of(j), J.p.roi, J.p.oht, J.p.tht, J.p.ntests, base + J.o_vix,
+                               base + o_tabs + J.o_tab, J.vp, J.g.blocksize, J.g.nblocks,
+                               J.g.nwantedperblock, obs_of(j),
+                               reinterpret_cast<int *>(base + J.o_err)});
+    }
+    // automatic: multi-job grids where the wave's jobs are small (many
+    // grids of a few waves of CTAs each, whose tails the merged grid
+    // removes: 64 jobs of 256^2-512^2, 43.1 -> 40.0 ms), per-job launches for
+    // larger jobs, whose grids already fill the GPU (the 64-DEM mix of
+    // 512^2-2048^2: equal when launched directly, 6 ms slower as a graph)
+    double cells = 0;
+    for (int j : waves[w]) cells += (double)jobs[j].n * jobs[j].n;
+    const bool merged = ctx->batch_mode == kBatchMerged ||
+                        (ctx->batch_mode == kBatchAuto && cells <= waves[w].size() * 1048576.0);
+    if (merged) {
+      CK(launch_vix_queue(qjobs.data(), (int)qjobs.size(), st));
+      CK(launch_findmax_queue(qjobs.data(), (int)qjobs.size(), st));
+    } else {
+      for (int j : waves[w]) {
+        const Job &J = jobs[j];
+        CK(launch_vix(dem_of(j), J.p.roi, J.p.oht, J.p.tht, J.p.ntests, base + J.o_vix,
+                      base + o_tabs + J.o_tab, J.vp, reinterpret_cast<int *>(base + J.o_err), st));
+        CK(launch_findmax(base + J.o_vix, J.n, J.g.blocksize, J.g.nblocks, J.g.nwantedperblock,
+                          obs_of(j), st));
+      }
+    }
+    // VIEWSHED: one launch per job, its CTA sized to the job's rays (one ray
+    // a thread), so CTAs of every job's size pack the SMs
+    for (int j : waves[w]) {
+      const Job &J = jobs[j];
       CK(launch_sheds(dem_of(j), J.p.roi, J.p.oht, J.p.tht, J.g.nwanted, obs_of(j),
-                      reinterpret_cast<uint64_t *>(base + J.o_sheds), J.sp, err, st));
+                      reinterpret_cast<uint64_t *>(base + J.o_sheds), J.sp,
+                      reinterpret_cast<int *>(base + J.o_err), st));
     }
     CK(cudaEventRecord(ctx->wave_ev[w], st));
   }
-  CK(cudaEventRecord(ctx->ev[1], st));
+  CK(cudaEventRecordWithFlags(ctx->ev[1], st, rec_flags));
   for (size_t w = 0; w < waves.size(); w++) {
     CK(cudaStreamWaitEvent(st2, ctx->wave_ev[w], 0));
     std::vector<SiteJob> sj;
@@ -273,8 +362,9 @@ int run_batch(siting_ctx *ctx, int njobs, const siting_params *params,
     CK(launch_site_jobs(sj.data(), (int)sj.size(), base + o_wtabs + o_wtab[w],
                         stage + s_wtabs + o_wtab[w], st2));
   }
-  CK(cudaEventRecord(ctx->ev[4], st2));
-  CK(cudaStreamWaitEvent(st, ctx->ev[4], 0));
+  CK(cudaEventRecordWithFlags(ctx->ev[4], st2, rec_flags));
+  CK(cudaEventRecord(ctx->ev[2], st2));  // the join of the SITE stream
+  CK(cudaStreamWaitEvent(st, ctx->ev[2], 0));
   // outputs and per-job readback (SITE outputs and error flag)
   long long *hout = reinterpret_cast<long long *>(stage + s_out);
   for (int j = 0; j < njobs; j++) {
@@ -285,7 +375,7 @@ int run_batch(siting_ctx *ctx, int njobs, const siting_params *params,
     CK(cudaMemcpyAsync(hout + 16 * j + 8, base + J.o_err, sizeof(int), cudaMemcpyDeviceToHost,
                        st));
   }
-  CK(cudaEventRecord(ctx->ev[6], st));
+  CK(cudaEventRecordWithFlags(ctx->ev[6], st, rec_flags));
   if (host_io)
     for (int j = 0; j < njobs; j++) {
       const Job &J = jobs[j];
@@ -293,10 +383,40 @@ int run_batch(siting_ctx *ctx, int njobs, const siting_params *params,
                          cudaMemcpyDeviceToHost, st));
       CK(cudaMemcpyAsync(sel_out[j], base + J.o_sel, J.g.nwanted, cudaMemcpyDeviceToHost, st));
     }
-  CK(cudaEventRecord(ctx->ev[7], st));
+  CK(cudaEventRecordWithFlags(ctx->ev[7], st, rec_flags));
+  return SITING_OK;
+  };
+
+  if (graph && ctx->bg_exec && key == ctx->bg_key) {
+    CK(cudaGraphLaunch(ctx->bg_exec, st));  // the same batch again: replay
+    ctx->bg_replays++;
+  } else if (graph) {
+    batch_graph_reset(ctx);
+    // capture mode ThreadLocal: other threads' CUDA calls are not affected
+    CK(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+    const int erc = enqueue(true);
+    cudaGraph_t g = nullptr;
+    const cudaError_t ce = cudaStreamEndCapture(st, &g);
+    cudaGraphExec_t exec = nullptr;
+    const bool ok = erc == SITING_OK && ce == cudaSuccess && g &&
+                    cudaGraphInstantiate(&exec, g, 0) == cudaSuccess;
+    if (g) cudaGraphDestroy(g);
+    if (ok) {
+      ctx->bg_exec = exec;
+      ctx->bg_key = key;
+      ctx->bg_captures++;
+      CK(cudaGraphLaunch(ctx->bg_exec, st));
+    } else {  // a capture the runtime refused: run the same work directly
+      cudaGetLastError();
+      if ((rc = enqueue(false))) return rc;
+    }
+  } else if ((rc = enqueue(false))) {
+    return rc;
+  }
   CK(cudaStreamSynchronize(st));
+  const long long *rout = reinterpret_cast<const long long *>(stage + s_out);
   std::vector<int> flags(njobs);
-  for (int j = 0; j < njobs; j++) flags[j] = (int)(hout[16 * j + 8] & 0xffffffff);
+  for (int j = 0; j < njobs; j++) flags[j] = (int)(rout[16 * j + 8] & 0xffffffff);
   for (int j = 0; j < njobs; j++)
     if (flags[j]) {
       rc = check_err_flags(ctx, &flags[j], 1);
@@ -308,15 +428,16 @@ int run_batch(siting_ctx *ctx, int njobs, const siting_params *params,
   cudaEventElapsedTime(&t[1], ctx->ev[0], ctx->ev[1]);  // VIX, FINDMAX, VIEWSHED of all jobs
   cudaEventElapsedTime(&t[4], ctx->ev[1], ctx->ev[4]);  // SITE after them
   cudaEventElapsedTime(&t[5], ctx->ev[6], ctx->ev[7]);
+  cudaGetLastError();  // a phase time that cannot be read stays 0 and leaves no error behind
   if (results)
     for (int j = 0; j < njobs; j++) {
       siting_result &r = results[j];
       r = siting_result{};
-      r.nusedsheds = (int)hout[16 * j];
-      r.cumarea = hout[16 * j + 1];
+      r.nusedsheds = (int)rout[16 * j];
+      r.cumarea = rout[16 * j + 1];
       r.coverage = 100.0 * r.cumarea / ((double)jobs[j].n * jobs[j].n);
       r.nwanted = jobs[j].g.nwanted;
-      r.site_rounds = (int)hout[16 * j + 2];
+      r.site_rounds = (int)rout[16 * j + 2];
       r.ms_h2d = t[0];  // batch-wide phase times
       r.ms_vix = t[1];  // VIX, FINDMAX and VIEWSHED of every job (SITE overlaps them)
       r.ms_findmax = 0.f;

@@ -40,6 +40,9 @@ struct BatchPlan {
 int plan_batch(int sm_count, int njobs, const siting_params *params, const siting_plan *plans,
                BatchPlan *bp, std::string *err);
 
+// Drops the context's captured batch graph (its workspace may be gone).
+void batch_graph_reset(siting_ctx *ctx);
+
 // Runs a batch.  src_pitch (elements, may be null; 0 = nrows) is the row
 // pitch of each job's DEM; host_io selects host or device buffers.
 int run_batch(siting_ctx *ctx, int njobs, const siting_params *params,

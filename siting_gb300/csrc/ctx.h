@@ -18,6 +18,9 @@ struct DevBuf {
 
 enum Slot { kDem, kVix, kObs, kSheds, kTables, kSite, kSel, kErr, kBatch, kNumSlots };
 
+// How a batch launches VIX and FINDMAX (siting_ctx_set_batch_mode).
+enum BatchMode { kBatchAuto = 0, kBatchMerged = 1, kBatchPerJob = 2 };
+
 // Launch plan measured fastest by siting_autotune for (roi, ntests).
 struct TunedPlan {
   int roi, ntests;
@@ -36,6 +39,7 @@ struct siting_ctx {
   cudaEvent_t ev[8] = {};
   std::string err;
   int site_ctas = 0;                  // 0 = automatic
+  int batch_mode = 0;                 // siting::BatchMode
   int tab_roi = -1, tab_ntests = -1;  // VIX tables currently on the device
   std::vector<unsigned char> tab_host;
   long long *h_out = nullptr;         // pinned: SITE outputs
@@ -46,6 +50,12 @@ struct siting_ctx {
   std::vector<siting::TunedPlan> tuned;  // autotuned plans, used when no plan is given
   cudaStream_t stream2 = nullptr;         // batches: SITE launches, overlapping `stream`
   std::vector<cudaEvent_t> wave_ev;       // batches: one per SITE launch
+  bool batch_graphs = true;               // device-resident batches run as CUDA graphs
+  cudaGraphExec_t bg_exec = nullptr;      // the last captured batch
+  std::vector<unsigned char> bg_key;      // its jobs, buffers and workspace
+  unsigned char *bg_stage = nullptr;      // its pinned host staging
+  size_t bg_stage_cap = 0;
+  long long bg_captures = 0, bg_replays = 0;
 };
 
 namespace siting {

@@ -1,71 +1,49 @@
 // FINDMAX: tentative observers, nwantedperblock per block
-// (siting.cpp:204-241).
-//
-// Block (bx,by) spans rows [(int)(bs*bx), min((int)(bs*(bx+1)), n)) and the
-// same for columns.  Each round picks the block cell with the largest
-// (vix, h), h = x*(x+y)*010101010101 wrapping in int32; among equal (vix, h)
-// the first cell of the row-major scan wins.  The winner goes to
-// obs[block*npb + round] and its vix is cleared, so a later round can pick a
-// cleared cell again once every cell is zero.
-//
-// GB300 mapping: one warp per block.  Each lane folds its strided subset of
-// the block into one 64-bit key (vix:8 | h^0x80000000:32 | 0xFFFFFF-j:24,
-// j < 3000^2 < 2^24 is the row-major position), so an unsigned max over the
-// warp (shuffles) gives exactly the reference's winner and tie-break.
+// (siting.cpp:204-241), one warp per block (findmax_dev.cuh).
 #include "common.cuh"
+#include "findmax_dev.cuh"
 #include "kernels.h"
 
 namespace siting {
 namespace {
 
-__device__ __forceinline__ unsigned long long warp_max_u64(unsigned long long v) {
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) {
-    const unsigned long long w = __shfl_xor_sync(0xffffffffu, v, o);
-    v = w > v ? w : v;
-  }
-  return v;
-}
-
 __global__ void __launch_bounds__(256) findmax_kernel(uint8_t *vix, int n, float bs, int nb,
                                                       int npb, int32_t *obs) {
   const int b = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  const int lane = threadIdx.x & 31;
   if (b >= nb * nb) return;
-  const int bx = b / nb, by = b - (b / nb) * nb;
-  const int x0 = f2i(fmul(bs, i2f(bx))), y0 = f2i(fmul(bs, i2f(by)));
-  const int x1 = min(f2i(fmul(bs, i2f(bx + 1))), n);
-  const int y1 = min(f2i(fmul(bs, i2f(by + 1))), n);
-  const int w = y1 - y0, npts = (x1 - x0) * w;
-  for (int k = 0; k < npb; k++) {
-    unsigned long long best = 0;
-    // walk j = lane, lane+32, ... keeping (row, col) incrementally
-    int r = lane / max(w, 1), c = lane - r * w;
-    for (int j = lane; j < npts; j += 32) {
-      const int x = x0 + r, y = y0 + c;
-      const unsigned v = vix[x * n + y];
-      const unsigned h = (unsigned)x * (unsigned)(x + y) * 0x41041041u;
-      const unsigned long long key = ((unsigned long long)v << 56) |
-                                     ((unsigned long long)(h ^ 0x80000000u) << 24) |
-                                     (unsigned long long)(0xFFFFFF - j);
-      best = key > best ? key : best;
-      c += 32;
-      while (c >= w) {
-        c -= w;
-        r++;
-      }
-    }
-    best = warp_max_u64(best);
-    // an empty block keeps the scan's starting cell (xmin, ymin), as the
-    // reference's loop does when it never runs
-    const int j = npts > 0 ? 0xFFFFFF - (int)(best & 0xFFFFFFull) : 0;
-    const int x = npts > 0 ? x0 + j / w : x0, y = npts > 0 ? y0 + j % w : y0;
-    if (lane == 0) {
-      obs[(size_t)b * npb + k] = x * n + y;
-      if (x < n && y < n) vix[x * n + y] = 0;
-    }
-    __syncwarp();
+  findmax_block(vix, n, bs, nb, npb, obs, b, threadIdx.x & 31);
+}
+
+// FINDMAX of many jobs in one grid (batched form): one warp per (job, block)
+// item; the job table is the kernel's parameters and a warp finds its job
+// from its index.
+struct FindmaxQJob {
+  uint8_t *vix;
+  int32_t *obs;
+  int n, nb, npb;
+  float bs;
+  unsigned first;  // warp index of the job's first block
+};
+struct FindmaxQTable {
+  FindmaxQJob jobs[kStageQueueMaxJobs];
+  int njobs;
+  unsigned total;
+};
+
+__global__ void __launch_bounds__(256) findmaxq_kernel(const __grid_constant__ FindmaxQTable tab) {
+  const unsigned it = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  if (it >= tab.total) return;
+  int lo = 0, hi = tab.njobs - 1;  // the last job whose first block is at or before `it`
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (tab.jobs[mid].first <= it)
+      lo = mid;
+    else
+      hi = mid - 1;
   }
+  const FindmaxQJob &J = tab.jobs[lo];
+  findmax_block(J.vix, J.n, J.bs, J.nb, J.npb, J.obs, (int)(it - J.first),
+                       threadIdx.x & 31);
 }
 
 // Flags observer indices outside [0, n*n).
@@ -82,6 +60,26 @@ cudaError_t launch_check_obs(const int32_t *obs, int nsheds, int nrows, int *d_e
   const int grid = (nsheds + 255) / 256 < 1024 ? (nsheds + 255) / 256 : 1024;
   check_obs_kernel<<<grid, 256, 0, st>>>(obs, nsheds, (long long)nrows * nrows, d_err);
   return cudaGetLastError();
+}
+
+cudaError_t launch_findmax_queue(const StageJob *jobs, int njobs, cudaStream_t st) {
+  static thread_local FindmaxQTable tab;
+  int j = 0;
+  while (j < njobs) {
+    tab.njobs = 0;
+    tab.total = 0;
+    for (; j < njobs && tab.njobs < kStageQueueMaxJobs; j++) {
+      const StageJob &J = jobs[j];
+      tab.jobs[tab.njobs++] =
+          FindmaxQJob{J.vix, J.obs, J.dem.nrows, J.nb, J.npb, J.bs, tab.total};
+      tab.total += (unsigned)(J.nb * J.nb);
+    }
+    const long long grid = ((long long)tab.total * 32 + 255) / 256;
+    findmaxq_kernel<<<(unsigned)grid, 256, 0, st>>>(tab);
+    const cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+  }
+  return cudaSuccess;
 }
 
 cudaError_t launch_findmax(uint8_t *vix, int nrows, float blocksize, int nblocks, int npb,

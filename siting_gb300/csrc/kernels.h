@@ -69,6 +69,28 @@ cudaError_t launch_sheds(const DemView &dem, int roi, int oht, int tht, int nshe
                          const int32_t *obs, uint64_t *sheds, const ShedPlan &plan, int *d_err,
                          cudaStream_t st);
 
+// ---- many jobs per launch (batched form) ---------------------------------------
+// One job of a multi-job launch: its DEM, VIX and FINDMAX arguments and buffers.
+struct StageJob {
+  DemView dem;
+  int roi, oht, tht, ntests;
+  uint8_t *vix;
+  const void *vix_tables;  // vix_fill_tables layout on the device
+  VixPlan vplan;
+  float bs;                // FINDMAX block geometry
+  int nb, npb;
+  int32_t *obs;
+  int *err;
+};
+// Jobs per multi-job launch (the job table is the kernel's parameters).
+constexpr int kStageQueueMaxJobs = 64;
+// VIX of every tile of `jobs`: one grid over the (job, tile) items of the
+// jobs whose halo is staged and one over the others (more when a kind has
+// over kStageQueueMaxJobs jobs).
+cudaError_t launch_vix_queue(const StageJob *jobs, int njobs, cudaStream_t st);
+// FINDMAX of every block of `jobs`: one grid over the (job, block) items.
+cudaError_t launch_findmax_queue(const StageJob *jobs, int njobs, cudaStream_t st);
+
 // ---- SITE -----------------------------------------------------------------------
 // Scratch layout of one SITE job (device, carved from one allocation).
 struct SiteScratch {

@@ -1301,7 +1301,27 @@ cudaError_t launch_site_jobs(const SiteJob *jobs, int njobs, void *d_table, void
   const SiteArgs *d_args = static_cast<const SiteArgs *>(d_table);
   const int *d_map = reinterpret_cast<const int *>(static_cast<unsigned char *>(d_table) + off);
   void *kargs[] = {&d_args, &d_map};
-  return cudaLaunchCooperativeKernel(kern, dim3(total), dim3(threads), kargs, shm, st);
+  // cooperative (its CTAs wait for one another at group barriers, so all must
+  // be resident) and at the device's highest priority, carried by the launch
+  // itself so that a CUDA graph captured from the stream keeps it: the block
+  // scheduler then gives a SITE launch SMs as the CTAs of concurrent stage
+  // kernels end
+  int least = 0, greatest = 0;
+  e = cudaDeviceGetStreamPriorityRange(&least, &greatest);
+  if (e != cudaSuccess) return e;
+  cudaLaunchAttribute attr[2];
+  attr[0].id = cudaLaunchAttributeCooperative;
+  attr[0].val.cooperative = 1;
+  attr[1].id = cudaLaunchAttributePriority;
+  attr[1].val.priority = greatest;
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(total);
+  cfg.blockDim = dim3(threads);
+  cfg.dynamicSmemBytes = shm;
+  cfg.stream = st;
+  cfg.attrs = attr;
+  cfg.numAttrs = 2;
+  return cudaLaunchKernelExC(&cfg, kern, kargs);
 }
 
 cudaError_t launch_site(int nrows, int roi, int intervis, int nsheds, const int32_t *obs,

@@ -135,6 +135,7 @@ template <bool kInterior, class Dem>
 __device__ __forceinline__ void vix_tile_work(const Dem &dem, const VixArgs &a,
                                               const int4 *cinfo, const uint2 *jump,
                                               const unsigned long long *rtab2, int *cnt) {
+
   const int ncell = a.tile * a.tile;
   const int L = max(1, (int)blockDim.x / ncell);  // a power of two: tiles are 16, 32, 64
   const int per_pass = blockDim.x / L;
@@ -164,21 +165,22 @@ __device__ __forceinline__ void vix_tile_work(const Dem &dem, const VixArgs &a,
   }
 }
 
+// One T x T tile of cells: `map` is the halo's tensor map (kSmem), `tile` the
+// tile's index (row-major over tiles_per_row^2), `sm` the CTA's dynamic
+// shared memory (vix_smem_bytes), `mbar` the halo's mbarrier (shared
+// memory).  Every thread of the CTA calls it.
 template <bool kSmem>
-__global__ void __launch_bounds__(1024) vix_kernel(const __grid_constant__ CUtensorMap map,
-                                                  const VixArgs a) {
-  extern __shared__ __align__(128) unsigned char sm[];
+__device__ __forceinline__ void vix_tile(const CUtensorMap *map, const VixArgs &a, int tile,
+                                         unsigned char *sm, uint64_t *mbar) {
   const int T = a.tile;
-  const int tx0 = (blockIdx.x / a.tiles_per_row) * T;
-  const int ty0 = (blockIdx.x % a.tiles_per_row) * T;
+  const int tx0 = (tile / a.tiles_per_row) * T;
+  const int ty0 = (tile % a.tiles_per_row) * T;
   const int hx0 = tx0 - a.roi;
   const int hy0 = (ty0 - a.roi) & ~7;  // TMA inner coordinate: 16-byte aligned
   size_t off = 0;
   uint16_t *halo = reinterpret_cast<uint16_t *>(sm);
   const uint32_t halo_bytes = kSmem ? (uint32_t)a.nboxes * a.box_rows * a.halo_w * 2u : 0u;
-  off += halo_bytes;
-  uint64_t *mbar = reinterpret_cast<uint64_t *>(sm + off);
-  off += 16;
+  off += halo_bytes + 16;  // (the per-tile kernel's mbarrier)
   uint2 *jump = reinterpret_cast<uint2 *>(sm + off);
   off += (size_t)a.ntests * 8;
   unsigned long long *rtab2 = reinterpret_cast<unsigned long long *>(sm + off);  // {r, r} pairs
@@ -194,7 +196,7 @@ __global__ void __launch_bounds__(1024) vix_kernel(const __grid_constant__ CUten
     mbar_init(mbar, 1);
     mbar_expect_tx(mbar, halo_bytes);
     for (int b = 0; b < a.nboxes; b++)
-      tma_load_window(halo + (size_t)b * a.box_rows * a.halo_w, &map, hy0, hx0 + b * a.box_rows,
+      tma_load_window(halo + (size_t)b * a.box_rows * a.halo_w, map, hy0, hx0 + b * a.box_rows,
                       mbar);
   }
   for (int i = threadIdx.x; i < a.ntests; i += blockDim.x)
@@ -246,6 +248,53 @@ __global__ void __launch_bounds__(1024) vix_kernel(const __grid_constant__ CUten
     const int x = tx0 + lx, y = ty0 + (i - lx * T);
     if (x < a.n && y < a.n) a.vix[x * a.n + y] = vtab[cnt[i]];
   }
+}
+
+template <bool kSmem>
+__global__ void __launch_bounds__(1024) vix_kernel(const __grid_constant__ CUtensorMap map,
+                                                  const VixArgs a) {
+  extern __shared__ __align__(128) unsigned char sm[];
+  const uint32_t halo_bytes = kSmem ? (uint32_t)a.nboxes * a.box_rows * a.halo_w * 2u : 0u;
+  vix_tile<kSmem>(&map, a, blockIdx.x, sm, reinterpret_cast<uint64_t *>(sm + halo_bytes));
+}
+
+// ---- VIX of many jobs in one launch (batched form) ---------------------------
+// One grid covers the (job, tile) items of many jobs, so a job's last tiles
+// overlap the next job's first ones instead of each job ending a grid of its
+// own.  The job table travels as the kernel's parameters, and a CTA finds its
+// job from its index: every value derived from the table is then the same in
+// all threads and is read from the constant bank, as in the one-job kernel.
+
+struct VixQJob {
+  CUtensorMap map;  // halo map of a staged job
+  VixArgs a;
+  unsigned first;   // grid index of the job's first tile
+};
+
+struct VixQTable {
+  VixQJob jobs[kStageQueueMaxJobs];
+  int njobs;
+};
+static_assert(sizeof(VixQTable) <= 32000, "kernel parameters are limited to 32 KB");
+
+// One CTA per (job, tile) item.  kSmem: every job of the launch has its halo
+// staged (else none has): one kernel per staging keeps each within 32
+// registers a thread.
+template <bool kSmem>
+__global__ void __launch_bounds__(1024, 2) vixq_kernel(const __grid_constant__ VixQTable tab) {
+  extern __shared__ __align__(128) unsigned char sm[];
+  __shared__ __align__(8) uint64_t mbar;
+  const unsigned it = blockIdx.x;
+  int lo = 0, hi = tab.njobs - 1;  // the last job whose first tile is at or before `it`
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (tab.jobs[mid].first <= it)
+      lo = mid;
+    else
+      hi = mid - 1;
+  }
+  const VixQJob &J = tab.jobs[lo];
+  vix_tile<kSmem>(&J.map, J.a, (int)(it - J.first), sm, &mbar);
 }
 
 int round8(int v) { return (v + 7) & ~7; }
@@ -341,8 +390,12 @@ VixPlan vix_plan_for(int nrows, int roi, int ntests, int tile, int smem) {
   return p;
 }
 
-cudaError_t launch_vix(const DemView &dem, int roi, int oht, int tht, int ntests, uint8_t *vix,
-                       const void *d_tables, const VixPlan &plan, int *d_err, cudaStream_t st) {
+namespace {
+
+// Kernel arguments and halo map of one job; false if the map cannot be made.
+bool vix_args(const DemView &dem, int roi, int oht, int tht, int ntests, uint8_t *vix,
+              const void *d_tables, const VixPlan &plan, int *d_err, VixArgs *out,
+              CUtensorMap *map, bool *smem) {
   VixArgs a{};
   a.dem = dem.data;
   a.pitch = dem.pitch;
@@ -358,16 +411,28 @@ cudaError_t launch_vix(const DemView &dem, int roi, int oht, int tht, int ntests
   a.rtab = reinterpret_cast<const float *>(a.jump + 2 * ntests);
   a.vtab = reinterpret_cast<const uint8_t *>(a.rtab + roi + 1);
   a.err = d_err;
-  CUtensorMap map;
-  memset(&map, 0, sizeof(map));
-  const bool smem = plan.use_smem && dem.tma_ok;
-  if (smem) {
+  memset(map, 0, sizeof(*map));
+  *smem = plan.use_smem && dem.tma_ok;
+  if (*smem) {
     const HaloGeom g = halo_geom(plan.tile, roi);
     a.halo_w = g.w;
     a.box_rows = g.box_rows;
     a.nboxes = g.nboxes;
-    if (!make_dem_tensor_map(&map, dem, g.w, g.box_rows)) return cudaErrorInvalidValue;
+    if (!make_dem_tensor_map(map, dem, g.w, g.box_rows)) return false;
   }
+  *out = a;
+  return true;
+}
+
+}  // namespace
+
+cudaError_t launch_vix(const DemView &dem, int roi, int oht, int tht, int ntests, uint8_t *vix,
+                       const void *d_tables, const VixPlan &plan, int *d_err, cudaStream_t st) {
+  VixArgs a;
+  CUtensorMap map;
+  bool smem;
+  if (!vix_args(dem, roi, oht, tht, ntests, vix, d_tables, plan, d_err, &a, &map, &smem))
+    return cudaErrorInvalidValue;
   VixPlan eff = plan;
   eff.use_smem = smem;
   const size_t shm = vix_smem_bytes(eff, roi, ntests);
@@ -385,6 +450,45 @@ cudaError_t launch_vix(const DemView &dem, int roi, int oht, int tht, int ntests
     vix_kernel<false><<<grid, plan.threads, shm, st>>>(map, a);
   }
   return cudaGetLastError();
+}
+
+cudaError_t launch_vix_queue(const StageJob *jobs, int njobs, cudaStream_t st) {
+  // jobs whose halo is staged, then those read through L1: one launch for
+  // each kind, at most kStageQueueMaxJobs jobs a launch
+  static thread_local VixQTable tab;  // 20 KB: not on the host stack
+  for (int kind = 0; kind < 2; kind++) {
+    int j = 0;
+    while (j < njobs) {
+      tab.njobs = 0;
+      size_t shm = 0;
+      unsigned total = 0;
+      for (; j < njobs && tab.njobs < kStageQueueMaxJobs; j++) {
+        const StageJob &J = jobs[j];
+        VixQJob &q = tab.jobs[tab.njobs];
+        memset(&q, 0, sizeof(q));
+        bool smem;
+        if (!vix_args(J.dem, J.roi, J.oht, J.tht, J.ntests, J.vix, J.vix_tables, J.vplan, J.err,
+                      &q.a, &q.map, &smem))
+          return cudaErrorInvalidValue;
+        if ((smem ? 0 : 1) != kind) continue;
+        q.first = total;
+        VixPlan eff = J.vplan;
+        eff.use_smem = smem;
+        shm = std::max(shm, vix_smem_bytes(eff, J.roi, J.ntests));
+        total += (unsigned)(q.a.tiles_per_row * q.a.tiles_per_row);
+        tab.njobs++;
+      }
+      if (!tab.njobs) continue;
+      auto kern = kind == 0 ? vixq_kernel<true> : vixq_kernel<false>;
+      cudaError_t e =
+          cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shm);
+      if (e != cudaSuccess) return e;
+      kern<<<total, 1024, shm, st>>>(tab);
+      e = cudaGetLastError();
+      if (e != cudaSuccess) return e;
+    }
+  }
+  return cudaSuccess;
 }
 
 }  // namespace siting

@@ -84,3 +84,64 @@ def test_batch_large_roi(ctx, oracle, native):
     out = ctx.run_batch([p for p, _ in jobs], [d for _, d in jobs])
     for (p, dem), (obs, sel, res) in zip(jobs, out):
         _check_job(oracle, p, dem, obs, sel, res)
+
+
+@pytest.mark.parametrize("mode", [1, 2])
+def test_batch_modes_match_oracle(ctx, oracle, native, mode):
+    """Multi-job VIX and FINDMAX grids (1) and one launch per stage and job
+    (2) give the same results; small block widths give many FINDMAX blocks
+    per job and non-multiple sides make blocks straddle VIX tiles."""
+    jobs = _mixed_jobs(native, 8, 6, sizes=(90, 300), rois=(5, 40))
+    for k, (n, bw, roi) in enumerate(((40, 1, 5), (97, 2, 9), (150, 3, 14), (211, 5, 20))):
+        dem = native.fbm_dem(n, 7700 + k, octaves=6, range_max=9000)
+        jobs[k] = (native.Params(nrows=n, roi=roi, height=25, ntests=32, bw=bw,
+                                 nwanted0=max(1, n * n // 64), intervis=k % 2), dem)
+    ctx.set_batch_mode(mode)
+    try:
+        out = ctx.run_batch([p for p, _ in jobs], [d for _, d in jobs])
+    finally:
+        ctx.set_batch_mode(0)
+    for (p, dem), (obs, sel, res) in zip(jobs, out):
+        _check_job(oracle, p, dem, obs, sel, res)
+
+
+def test_batch_graph_replay_matches_eager_and_oracle(ctx, oracle, native):
+    """The device-resident batch is captured as a CUDA graph on its first call
+    and replayed on the next identical one; a changed buffer is captured
+    anew; replays, eager launches and the oracle agree."""
+    torch = pytest.importorskip("torch")
+    jobs = _mixed_jobs(native, 6, 7)
+    params = [p for p, _ in jobs]
+    d_dems = [torch.from_numpy(d.view(np.int16)).cuda() for _, d in jobs]
+    geos = [native.block_geometry(p.nrows, p.bw, p.nwanted0) for p in params]
+    d_obs = [torch.empty(g.nwanted, dtype=torch.int32, device="cuda") for g in geos]
+    d_sel = [torch.empty(g.nwanted, dtype=torch.uint8, device="cuda") for g in geos]
+    torch.cuda.synchronize()
+    c0, r0 = ctx.batch_graph_stats()
+    res1 = ctx.run_batch_dev(params, d_dems, d_obs, d_sel)
+    obs1 = [o.cpu().numpy() for o in d_obs]
+    sel1 = [s.cpu().numpy() for s in d_sel]
+    for o, s in zip(d_obs, d_sel):
+        o.fill_(-1)
+        s.fill_(7)
+    torch.cuda.synchronize()
+    res2 = ctx.run_batch_dev(params, d_dems, d_obs, d_sel)
+    c1, r1 = ctx.batch_graph_stats()
+    assert (c1, r1) == (c0 + 1, r0 + 1), "second identical call should replay the graph"
+    for k in range(len(jobs)):
+        assert np.array_equal(d_obs[k].cpu().numpy(), obs1[k])
+        assert np.array_equal(d_sel[k].cpu().numpy(), sel1[k])
+        assert (res1[k].nusedsheds, res1[k].cumarea) == (res2[k].nusedsheds, res2[k].cumarea)
+    # a new output buffer for one job: captured again, same results
+    d_sel[0] = torch.zeros_like(d_sel[0])
+    ctx.run_batch_dev(params, d_dems, d_obs, d_sel)
+    assert ctx.batch_graph_stats()[0] == c1 + 1
+    assert np.array_equal(d_sel[0].cpu().numpy(), sel1[0])
+    ctx.set_batch_graphs(False)
+    try:
+        res3 = ctx.run_batch_dev(params, d_dems, d_obs, d_sel)
+    finally:
+        ctx.set_batch_graphs(True)
+    for k, ((p, dem), r) in enumerate(zip(jobs, res3)):
+        assert (r.nusedsheds, r.cumarea) == (res1[k].nusedsheds, res1[k].cumarea)
+        _check_job(oracle, p, dem, obs1[k], sel1[k], r)
