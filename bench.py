@@ -317,8 +317,8 @@ NCU_TRAFFIC = {
 # with roi 100 and 100 targets: per target for VIX, per observer for
 # VIEWSHED.  Keyed by the parameters they were measured with.
 ISSUE_WORK = {
-    ("vix", 100, 100): (2.10e9 / (2048 * 2048 * 100), "target"),
-    ("viewshed", 100, 100): (1.41e9 / 16384, "observer"),
+    ("vix", 100, 100): (2.058e9 / (2048 * 2048 * 100), "target"),
+    ("viewshed", 100, 100): (1.354e9 / 16384, "observer"),
 }
 ISSUE_SLOTS_PER_SM = 4  # one warp instruction per cycle from each SM sub-partition
 
@@ -697,11 +697,11 @@ def run_batch_workload(args):
     mb, mp = sum(tb) / len(tb), sum(tp) / len(tp)
     graph_stats = cb.batch_graph_stats()
     # the launch forms of the batch's VIX and FINDMAX (siting_ctx_set_batch_mode:
-    # 1 = grids over many jobs' items, 2 = one launch per job), captured as a
-    # CUDA graph and replayed, or launched directly
+    # 1 = grids over many jobs' items, 2 = one launch per job), the merged form
+    # also captured as a CUDA graph and replayed
     forms = {}
-    for name, mode, graphs in (("merged_grids_graph", 1, True), ("per_job_graph", 2, True),
-                               ("per_job_direct", 2, False), ("merged_grids_direct", 1, False)):
+    for name, mode, graphs in (("merged_grids_graph", 1, True), ("merged_grids_direct", 1, False),
+                               ("per_job_direct", 2, False)):
         cb.set_batch_mode(mode)
         cb.set_batch_graphs(graphs)
         for _ in range(2):
@@ -990,7 +990,8 @@ def main():
                                              "plain", "speedup_vs_plain",
                                              "bit_identical_to_plain", "batch_phase_ms",
                                              "plain_stage_ms_sum", "floor_ms",
-                                             "speedup_bound_vs_plain", "config")}
+                                             "speedup_bound_vs_plain", "graph",
+                                             "launch_forms_ms", "config")}
         sv = run_serve_workload(args)
         out["serving"] = {k: sv[k] for k in ("value", "unit", "latency_ms", "served", "refused",
                                              "requests_per_s", "gpu_busy_frac", "config",

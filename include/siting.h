@@ -121,11 +121,12 @@ int siting_ctx_set_site_ctas(siting_ctx *ctx, int nctas);
  * one FINDMAX launch per job, 0 = automatic: 1 for the SITE launches whose
  * jobs average at most 2^20 cells, else 2.  Results do not depend on it. */
 int siting_ctx_set_batch_mode(siting_ctx *ctx, int mode);
-/* Device-resident batches (siting_run_batch_dev) run as CUDA graphs (no
- * counterpart in the reference): the first call of a batch captures its
- * copies and launches, a later call with the same jobs, buffers and
- * workspace replays the graph (on = 1, the default); 0 launches every call
- * directly.  Results do not depend on it. */
+/* Device-resident batches (siting_run_batch_dev) whose VIX and FINDMAX all
+ * run as grids over many jobs (see siting_ctx_set_batch_mode) run as CUDA
+ * graphs (no counterpart in the reference): the first call of a batch
+ * captures its copies and launches, a later call with the same jobs, buffers
+ * and workspace replays the graph (on = 1, the default); 0 launches every
+ * call directly.  Results do not depend on it. */
 int siting_ctx_set_batch_graphs(siting_ctx *ctx, int on);
 /* Graphs captured and replayed by the context's batches so far. */
 int siting_ctx_batch_graph_stats(const siting_ctx *ctx, long long *captures,

@@ -220,11 +220,29 @@ int run_batch(siting_ctx *ctx, int njobs, const siting_params *params,
   }
   cudaStream_t st2 = ctx->stream2;
 
-  // The device-resident form runs as a CUDA graph: the first call of a batch
+  // VIX and FINDMAX launch form of each wave.  Automatic: grids over many
+  // jobs' items where the wave's jobs are small (many grids of a few waves of
+  // CTAs each, whose tails the merged grid removes: 64 jobs of 256^2-512^2,
+  // 43.1 -> 40.0 ms), one launch per job for larger jobs, whose grids already
+  // fill the GPU (the 64-DEM mix of 512^2-2048^2: equal).
+  std::vector<char> merged(waves.size());
+  for (size_t w = 0; w < waves.size(); w++) {
+    double cells = 0;
+    for (int j : waves[w]) cells += (double)jobs[j].n * jobs[j].n;
+    merged[w] = ctx->batch_mode == kBatchMerged ||
+                (ctx->batch_mode == kBatchAuto && cells <= waves[w].size() * 1048576.0);
+  }
+  // The device-resident form runs as a CUDA graph when every wave's VIX and
+  // FINDMAX are merged grids (batches of small jobs, whose launches a replay
+  // saves: 40.2 -> 40.0 ms on the 64 jobs above): the first call of a batch
   // captures its copies and launches, and a later call with the same jobs,
-  // buffers and workspace replays the graph.  The graph's host staging is
-  // its own pinned buffer, so nothing else overwrites what a replay copies.
-  const bool graph = !host_io && ctx->batch_graphs;
+  // buffers and workspace replays the graph.  (Batches with larger jobs run
+  // their launches directly: as a graph the 64-DEM mix took 240 ms against
+  // 234 ms, not explained.)  The graph's host staging is its own pinned
+  // buffer, so nothing else overwrites what a replay copies.
+  bool all_merged = true;
+  for (char mw : merged) all_merged = all_merged && mw;
+  const bool graph = !host_io && ctx->batch_graphs && all_merged;
   std::vector<unsigned char> key;
   if (graph) {
     auto put = [&](const void *p, size_t n) {
@@ -314,16 +332,7 @@ int run_batch(siting_ctx *ctx, int njobs, const siting_params *params,
                                J.g.nwantedperblock, obs_of(j),
                                reinterpret_cast<int *>(base + J.o_err)});
     }
-    // automatic: multi-job grids where the wave's jobs are small (many
-    // grids of a few waves of CTAs each, whose tails the merged grid
-    // removes: 64 jobs of 256^2-512^2, 43.1 -> 40.0 ms), per-job launches for
-    // larger jobs, whose grids already fill the GPU (the 64-DEM mix of
-    // 512^2-2048^2: equal when launched directly, 6 ms slower as a graph)
-    double cells = 0;
-    for (int j : waves[w]) cells += (double)jobs[j].n * jobs[j].n;
-    const bool merged = ctx->batch_mode == kBatchMerged ||
-                        (ctx->batch_mode == kBatchAuto && cells <= waves[w].size() * 1048576.0);
-    if (merged) {
+    if (merged[w]) {
       CK(launch_vix_queue(qjobs.data(), (int)qjobs.size(), st));
       CK(launch_findmax_queue(qjobs.data(), (int)qjobs.size(), st));
     } else {

@@ -1281,15 +1281,30 @@ cudaError_t launch_site_jobs(const SiteJob *jobs, int njobs, void *d_table, void
   int dev = 0, sms = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  // The scoring and the selection run at the device's highest priority,
+  // carried by each launch so that a CUDA graph captured from the stream
+  // keeps it: the block scheduler then gives them SMs as the CTAs of
+  // concurrent stage kernels end.
+  int least = 0, greatest = 0;
+  e = cudaDeviceGetStreamPriorityRange(&least, &greatest);
+  if (e != cudaSuccess) return e;
+  cudaLaunchAttribute prio;
+  prio.id = cudaLaunchAttributePriority;
+  prio.val.priority = greatest;
   for (int i = 0; i < njobs; i++) {  // round-1 gains of every job
     const SiteJob &j = jobs[i];
     if (j.nsheds <= 0) continue;
     const int nr = 2 * j.roi + 1, per = nr * ((nr + 63) / 64);
     const int sgrid = std::max(1, std::min(sms * 8, (j.nsheds + 7) / 8));
-    site_score_kernel<<<sgrid, 256, 0, st>>>(j.sheds, j.nsheds, per, j.scratch.gains);
+    cudaLaunchConfig_t sc = {};
+    sc.gridDim = dim3(sgrid);
+    sc.blockDim = dim3(256);
+    sc.stream = st;
+    sc.attrs = &prio;
+    sc.numAttrs = 1;
+    e = cudaLaunchKernelEx(&sc, site_score_kernel, j.sheds, j.nsheds, per, j.scratch.gains);
+    if (e != cudaSuccess) return e;
   }
-  e = cudaGetLastError();
-  if (e != cudaSuccess) return e;
   int threads = 512;
   for (int i = 0; i < njobs; i++)
     threads = std::max(threads, site_threads_for((jobs[i].nsheds + jobs[i].nctas - 1) /
@@ -1301,14 +1316,8 @@ cudaError_t launch_site_jobs(const SiteJob *jobs, int njobs, void *d_table, void
   const SiteArgs *d_args = static_cast<const SiteArgs *>(d_table);
   const int *d_map = reinterpret_cast<const int *>(static_cast<unsigned char *>(d_table) + off);
   void *kargs[] = {&d_args, &d_map};
-  // cooperative (its CTAs wait for one another at group barriers, so all must
-  // be resident) and at the device's highest priority, carried by the launch
-  // itself so that a CUDA graph captured from the stream keeps it: the block
-  // scheduler then gives a SITE launch SMs as the CTAs of concurrent stage
-  // kernels end
-  int least = 0, greatest = 0;
-  e = cudaDeviceGetStreamPriorityRange(&least, &greatest);
-  if (e != cudaSuccess) return e;
+  // cooperative: its CTAs wait for one another at group barriers, so all
+  // must be resident
   cudaLaunchAttribute attr[2];
   attr[0].id = cudaLaunchAttributeCooperative;
   attr[0].val.cooperative = 1;

@@ -162,12 +162,18 @@ __device__ __forceinline__ void sweep_rays(const Dem &dem, const ShedArgs &a, in
       // with no branch for the lanes of a warp to diverge on (window in
       // shared memory; through L1 the extra table read per step costs more).
       uint32_t rp = rcp + 4u;  // &rcp[|i|]
+      // the cell's shared-memory byte address, advanced by byte strides (no
+      // scaling of an element offset at every step)
+      uint32_t pbb = dem.s + 2u * (uint32_t)obase;
+      const int smajb = 2 * smaj, sminb = 2 * smin;
 #pragma unroll 2  // two steps a trip: half the loop tests and branches
       for (float fai = 1.f; fai <= fend; fai = fadd(fai, 1.f)) {  // fai = (float)|i|, exact
-        pb += smaj;
+        pbb += smajb;
         pos += dir;
         const int off = f2i(fadd(fmul(fai, sl), hsl));  // round(|i|*slope), half away from zero
-        const float fe = i2f(dem.at(pb + off * smin));
+        unsigned short ev;
+        asm("ld.shared.u16 %0, [%1];" : "=h"(ev) : "r"(pbb + off * sminb));
+        const float fe = i2f(ev);
         const float fa = __fsub_rn(fe, foalt);
         float y;
         asm("ld.shared.f32 %0, [%1];" : "=f"(y) : "r"(rp));
@@ -180,7 +186,7 @@ __device__ __forceinline__ void sweep_rays(const Dem &dem, const ShedArgs &a, in
         const unsigned long long V = f2_add(f2_pack(fe, foalt), f2_pack(ftht, t));
         if (f2_lo(V) >= f2_hi(V))
           asm volatile("red.shared.or.b32 [%0], %1;" ::"r"(img + 4u * (uint32_t)((off + roi) * stride + (pos >> 5))),
-                       "r"(1u << (pos & 31)) : "memory");
+                       "r"(__funnelshift_l(0u, 1u, pos)) : "memory");  // 1 << (pos & 31)
       }
     } else {
       for (float fai = 1.f; fai <= fend; fai = fadd(fai, 1.f)) {  // fai = (float)|i|, exact

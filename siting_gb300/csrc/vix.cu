@@ -107,12 +107,20 @@ __device__ __forceinline__ int vix_target(const Dem &dem, int obase, int n, int 
     // no branch is left for the lanes to diverge on.  (Through L1 the extra
     // loads cost more than the branch.)
     bool vis = true;
+    // the sample's shared-memory byte address, doubled about the observer's
+    // (no scaling of an element offset at every sample)
+    const uint32_t sb = smem_u32(dem.s);
+    uint32_t qb = sb + 2u * (uint32_t)q;
+    const uint32_t ob2 = sb + 2u * (uint32_t)obase;
+    const int sminb = 2 * smin;
     for (int step = 1; step < ad; step <<= 1) {
       const unsigned long long Q = f2_add(P, C);
       const int off = f2i(f2_lo(Q));  // round(slope*id), half away from zero
-      vis &= !(i2f(dem.at(q + off * smin)) > f2_hi(Q));
+      unsigned short ev;
+      asm("ld.shared.u16 %0, [%1];" : "=h"(ev) : "r"(qb + off * sminb));
+      vis &= !(i2f(ev) > f2_hi(Q));
       P = f2_add(P, P);
-      q = 2 * q - obase;  // id doubles
+      qb = 2u * qb - ob2;  // id doubles
     }
     return vis;
   } else {
