@@ -1,13 +1,16 @@
 // Batched form: many independent jobs (DEMs of any size and parameters) per
-// call.  VIX, FINDMAX and VIEWSHED of every job are enqueued back to back on
-// the context's stream (each job's grids are large: a tile or an observer per
-// CTA); the greedy SITE selections, whose dependent rounds leave most SMs
+// call.  The greedy SITE selections, whose dependent rounds leave most SMs
 // idle when run one job at a time, run many jobs at once: the jobs' CTA
-// groups are packed into as few cooperative launches as the SM count allows,
-// largest groups first, each group with its own barrier and scratch.  Each
-// such launch runs on a second stream as soon as its jobs' viewsheds exist,
-// so the selections overlap the later jobs' stages.  One workspace holds
-// every job's buffers; results are collected after a single synchronisation.
+// groups are packed into as few cooperative launches ("waves") as the SM
+// count allows, largest groups first, each group with its own barrier and
+// scratch.  The stages of each wave's jobs are enqueued on the context's
+// stream in wave order: VIX and FINDMAX as grids over all the wave's jobs'
+// items (small jobs) or one launch per job, then one VIEWSHED launch per job;
+// each SITE launch runs on a second stream as soon as its jobs' viewsheds
+// exist, so the selections overlap the later waves' stages.  One workspace
+// holds every job's buffers; results are collected after a single
+// synchronisation.  A device-resident batch of small jobs is captured as a
+// CUDA graph and replayed when the same batch comes again.
 #include <algorithm>
 #include <numeric>
 #include <vector>
