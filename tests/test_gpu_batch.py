@@ -145,3 +145,10 @@ def test_batch_graph_replay_matches_eager_and_oracle(ctx, oracle, native):
     for k, ((p, dem), r) in enumerate(zip(jobs, res3)):
         assert (r.nusedsheds, r.cumarea) == (res1[k].nusedsheds, res1[k].cumarea)
         _check_job(oracle, p, dem, obs1[k], sel1[k], r)
+
+
+def test_batch_knobs_reject_bad_values(ctx, native):
+    for mode in (-1, 3):
+        with pytest.raises(native.SitingError):
+            ctx.set_batch_mode(mode)
+    assert native.load().siting_ctx_set_batch_graphs(ctx.h, 2) == native.EINVAL

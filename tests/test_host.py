@@ -169,3 +169,14 @@ def test_noalloc_site_checks_arguments_on_the_host(native):
     assert lib.siting_site_it_noalloc(100, 10, 0, 5, None, buf, buf, None, C.byref(res)) == 1
     assert lib.siting_site_it_noalloc(100, 10, 1, 0, None, None, None, None, C.byref(res)) == 0
     assert (res.nusedsheds, res.cumarea, res.site_rounds) == (0, 0, 0)
+
+
+def test_batch_knobs_reject_a_missing_context(native):
+    """The batched form's knobs check their context before anything else."""
+    import ctypes as C
+
+    lib = native.load()
+    c, r = C.c_longlong(), C.c_longlong()
+    assert lib.siting_ctx_set_batch_mode(None, 1) == native.EINVAL
+    assert lib.siting_ctx_set_batch_graphs(None, 1) == native.EINVAL
+    assert lib.siting_ctx_batch_graph_stats(None, C.byref(c), C.byref(r)) == native.EINVAL
