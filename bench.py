@@ -683,6 +683,18 @@ def run_batch_workload(args):
 
     batched = lambda: cb.run_batch_dev(params, d_dems, obs_b, sel_b)  # noqa: E731
     plain = lambda: [cp.run_dev(p, d, o, s) for p, d, o, s in zip(params, d_dems, obs_p, sel_p)]  # noqa: E731
+    if args.batch_mode is not None:
+        cb.set_batch_mode(args.batch_mode)
+    if args.batch_only:  # the batched form alone (a launch list of its kernels)
+        for _ in range(args.warmup):
+            timed(sb, batched)
+        tb = [timed(sb, batched)[0] for _ in range(args.steps)]
+        cb.close()
+        cp.close()
+        return {"metric": METRIC + " (batched)", "value": cells / (sum(tb) / len(tb) / 1e3),
+                "unit": "cells/s", "ms_per_step": sum(tb) / len(tb), "steps": args.steps,
+                "warmup": args.warmup, "config": {"workload": f"batch{len(jobs)}_512_2048",
+                                                  "batch_mode": args.batch_mode}}
     for _ in range(args.warmup):
         timed(sb, batched)
         timed(spl, plain)
@@ -924,6 +936,10 @@ def main():
     ap.add_argument("--no-extras", action="store_true",
                     help="headline job only: no batched or serving measurements")
     ap.add_argument("--batch-jobs", type=int, default=64)
+    ap.add_argument("--batch-only", action="store_true",
+                    help="batched workload: time the batched form alone (no plain runs)")
+    ap.add_argument("--batch-mode", type=int, default=None, choices=[0, 1, 2],
+                    help="batched workload: VIX/FINDMAX launch form (siting_ctx_set_batch_mode)")
     ap.add_argument("--autotune", action="store_true",
                     help="time the launch plans on a corner of the DEM first (siting_autotune)")
     ap.add_argument("--autotune-rows", type=int, default=1024)
