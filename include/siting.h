@@ -119,7 +119,7 @@ int siting_ctx_set_site_ctas(siting_ctx *ctx, int nctas);
  * grid over their (job, tile) VIX items (two when some halos are staged and
  * some not) and one over their (job, block) FINDMAX items, 2 = one VIX and
  * one FINDMAX launch per job, 0 = automatic: 1 for the SITE launches whose
- * jobs average at most 2^20 cells, else 2.  Results do not depend on it. */
+ * jobs average at most 2^18 cells, else 2.  Results do not depend on it. */
 int siting_ctx_set_batch_mode(siting_ctx *ctx, int mode);
 /* Device-resident batches (siting_run_batch_dev) whose VIX and FINDMAX all
  * run as grids over many jobs (see siting_ctx_set_batch_mode) run as CUDA

@@ -33,7 +33,7 @@ int batch_site_ctas(int nsheds, int sm_count) {
   return std::min(std::min(g, std::max(1, nsheds)), sm_count);
 }
 
-constexpr int kBatchWaveCtas = 64;
+constexpr int kBatchWaveCtas = 96;
 
 bool site_fits(const Job &J, int G) {
   return site_smem_bytes(J.p.roi, J.g.nwanted, G, J.g.nblocks, J.g.nwantedperblock,
@@ -88,7 +88,8 @@ int plan_batch(int sm_count, int njobs, const siting_params *params, const sitin
   });
   // A SITE CTA fills its SM's register file, so a launch holds its SMs
   // alone: waves take at most kBatchWaveCtas SMs, leaving the rest to the
-  // later jobs' stages that the waves overlap.
+  // later jobs' stages that the waves overlap (the last wave, which runs after
+  // every stage, may take them all below).
   const int wave_cap = std::min(sm_count, kBatchWaveCtas);
   std::vector<std::vector<int>> &waves = bp->waves;
   std::vector<int> &wave_ctas = bp->wave_ctas;
@@ -106,9 +107,12 @@ int plan_batch(int sm_count, int njobs, const siting_params *params, const sitin
   }
   // a wave lasts as long as its slowest group: SMs a wave leaves free go to
   // its automatically planned groups in proportion to their candidates (a
-  // group's rounds shorten with more CTAs), up to the single-job default
+  // group's rounds shorten with more CTAs), up to the single-job default.
+  // The last wave runs after every job's stages, with nothing to share the
+  // GPU with: it may grow to every SM (64 jobs of 256^2-512^2: 39.9 ->
+  // 26.3 ms; the 64-DEM mix of 512^2-2048^2 with waves of 96: 231 ms).
   for (size_t w = 0; w < waves.size(); w++) {
-    const int spare = wave_cap - wave_ctas[w];
+    const int spare = (w + 1 == waves.size() ? sm_count : wave_cap) - wave_ctas[w];
     double total = 0;
     for (int j : waves[w])
       if (jobs[j].auto_G) total += jobs[j].g.nwanted;
@@ -224,20 +228,21 @@ int run_batch(siting_ctx *ctx, int njobs, const siting_params *params,
   cudaStream_t st2 = ctx->stream2;
 
   // VIX and FINDMAX launch form of each wave.  Automatic: grids over many
-  // jobs' items where the wave's jobs are small (many grids of a few waves of
-  // CTAs each, whose tails the merged grid removes: 64 jobs of 256^2-512^2,
-  // 43.1 -> 40.0 ms), one launch per job for larger jobs, whose grids already
-  // fill the GPU (the 64-DEM mix of 512^2-2048^2: equal).
+  // jobs' items where the wave's jobs average at most 2^18 cells (many grids
+  // of a few waves of CTAs each, whose tails the merged grid removes: 64 jobs
+  // of 256^2-512^2, 29.9 -> 26.3 ms), one launch per job for larger jobs,
+  // whose grids already fill the GPU (256^2-1024^2: 69.1 vs 66.5 ms merged
+  // and per job; 512^2-2048^2: 231.3 vs 230.4 ms).
   std::vector<char> merged(waves.size());
   for (size_t w = 0; w < waves.size(); w++) {
     double cells = 0;
     for (int j : waves[w]) cells += (double)jobs[j].n * jobs[j].n;
     merged[w] = ctx->batch_mode == kBatchMerged ||
-                (ctx->batch_mode == kBatchAuto && cells <= waves[w].size() * 1048576.0);
+                (ctx->batch_mode == kBatchAuto && cells <= waves[w].size() * 262144.0);
   }
   // The device-resident form runs as a CUDA graph when every wave's VIX and
   // FINDMAX are merged grids (batches of small jobs, whose launches a replay
-  // saves: 40.2 -> 40.0 ms on the 64 jobs above): the first call of a batch
+  // saves): the first call of a batch
   // captures its copies and launches, and a later call with the same jobs,
   // buffers and workspace replays the graph.  (Batches with larger jobs run
   // their launches directly: as a graph the 64-DEM mix took 240 ms against
