@@ -67,7 +67,10 @@ typedef struct siting_geometry {
 typedef struct siting_plan {
   int vix_tile;     /* VIX cell tile side: 16, 32 or 64 (0 = default) */
   int vix_smem;     /* 1: stage the DEM halo by TMA, 0: read through L1, -1: default */
-  int shed_smem;    /* 1: stage the observer window by TMA, 0: L1, -1: default */
+  int shed_smem;    /* VIEWSHED window: 1 two half windows staged by TMA, one
+                       CTA each (up to roi 151, else as 2), 2 the whole window
+                       in one CTA, staged up to roi 100, 0 the whole window
+                       through L1, -1 default (1 for roi 60..151, else 2) */
   int site_ctas;    /* CTAs of the job's SITE group (0 = default) */
 } siting_plan;
 
@@ -256,8 +259,8 @@ int siting_selftest_wait(siting_ctx *ctx, int which, long long max_cycles);
 
 /* ---- autotuner -----------------------------------------------------------
  * No counterpart in the reference.  Times the launch plans of each stage
- * (VIX tile 16/32/64 with the halo staged or read through L1; VIEWSHED window
- * staged or not; SITE group size when the sample is the whole DEM) on the
+ * (VIX tile 16/32/64 with the halo staged or read through L1; VIEWSHED half
+ * windows, the whole window staged, or read through L1; SITE group size when the sample is the whole DEM) on the
  * top-left sample_rows x sample_rows corner of the host DEM elevs (0 = 1024)
  * with p's parameters, and keeps the fastest for (roi, ntests) in the
  * context: later calls given no plan (siting_run*, siting_run_batch* with
@@ -265,6 +268,11 @@ int siting_selftest_wait(siting_ctx *ctx, int which, long long max_cycles);
  * it.  Results never depend on the plan. */
 int siting_autotune(siting_ctx *ctx, const siting_params *p,
                     const uint16_t *elevs, int sample_rows, siting_plan *best);
+/* Keeps *plan for jobs with this (roi, ntests) as if the autotuner had chosen
+ * it (a plan tuned in an earlier process, say); the stage functions take the
+ * plan of their roi whatever its ntests.  SITING_EINVAL for a field out of
+ * range. */
+int siting_autotune_set(siting_ctx *ctx, int roi, int ntests, const siting_plan *plan);
 /* Forgets every autotuned plan of the context. */
 int siting_autotune_clear(siting_ctx *ctx);
 

@@ -179,6 +179,7 @@ def load() -> C.CDLL:
         "siting_run_batch_dev": ([_P, i, _P, _P, _P, _P, _P, _P], i),
         "siting_batch_workspace_bytes": ([_P, i, _P, _P, C.POINTER(sz)], i),
         "siting_autotune": ([_P, C.POINTER(_ParamsC), _P, i, C.POINTER(_PlanC)], i),
+        "siting_autotune_set": ([_P, i, i, C.POINTER(_PlanC)], i),
         "siting_autotune_clear": ([_P], i),
         "siting_selftest_wait": ([_P, i, ll], i),
         "siting_server_create": ([i, sz, i, i, C.POINTER(_P)], i),
@@ -467,6 +468,11 @@ class Context:
         (0: SITE group barrier, 1: TMA mbarrier): ETIMEOUT when it expired as
         designed.  Does not raise."""
         return self._lib.siting_selftest_wait(self.h, which, max_cycles)
+
+    def autotune_set(self, roi: int, ntests: int, plan: Plan):
+        """Keep `plan` for jobs with this (roi, ntests), as a tuned plan."""
+        pc = plan.c()
+        self._check(self._lib.siting_autotune_set(self.h, roi, ntests, C.byref(pc)))
 
     def autotune_clear(self):
         self._check(self._lib.siting_autotune_clear(self.h))

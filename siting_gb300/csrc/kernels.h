@@ -61,6 +61,7 @@ cudaError_t launch_check_obs(const int32_t *obs, int nsheds, int nrows, int *d_e
 struct ShedPlan {
   int threads;
   bool use_smem;  // stage the (2roi+1)^2 window by TMA
+  bool half;      // two CTAs an observer, each staging the rows on one side of it
 };
 ShedPlan shed_default_plan(int roi);
 ShedPlan shed_plan_for(int roi, int smem);

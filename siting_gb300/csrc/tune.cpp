@@ -107,9 +107,14 @@ extern "C" int siting_autotune(siting_ctx *ctx, const siting_params *p, const ui
   CK(launch_findmax(static_cast<uint8_t *>(d_vix), n, g.blocksize, g.nblocks, g.nwantedperblock,
                     static_cast<int32_t *>(d_obs), st));
   bt = 1e30f;
-  for (int sm : {1, 0}) {
+  std::vector<ShedPlan> tried;
+  for (int sm : {1, 2, 0}) {
     const ShedPlan sp = shed_plan_for(p->roi, sm);
-    if (sm == 0 && out.shed_smem == 0) continue;  // staging unavailable: same plan
+    bool seen = false;  // the same plan under another setting
+    for (const ShedPlan &q : tried)
+      seen |= q.threads == sp.threads && q.use_smem == sp.use_smem && q.half == sp.half;
+    if (seen) continue;
+    tried.push_back(sp);
     float t;
     rc = time_ms(ctx, [&] {
       return launch_sheds(dem, p->roi, p->oht, p->tht, g.nwanted, static_cast<int32_t *>(d_obs),
@@ -118,7 +123,7 @@ extern "C" int siting_autotune(siting_ctx *ctx, const siting_params *p, const ui
     if (rc) return rc;
     if (t < bt) {
       bt = t;
-      out.shed_smem = sp.use_smem ? 1 : 0;
+      out.shed_smem = sm;
     }
   }
   // SITE group size, only when the sample is the whole job (its rounds and
@@ -166,6 +171,21 @@ extern "C" int siting_autotune(siting_ctx *ctx, const siting_params *p, const ui
     }
   if (!found) ctx->tuned.push_back(TunedPlan{p->roi, p->ntests, out});
   if (best) *best = out;
+  return SITING_OK;
+}
+
+extern "C" int siting_autotune_set(siting_ctx *ctx, int roi, int ntests, const siting_plan *plan) {
+  if (!ctx || !plan || roi < 0 || ntests < 0) return SITING_EINVAL;
+  const siting_plan &q = *plan;
+  if ((q.vix_tile != 0 && q.vix_tile != 16 && q.vix_tile != 32 && q.vix_tile != 64) ||
+      q.vix_smem < -1 || q.vix_smem > 1 || q.shed_smem < -1 || q.shed_smem > 2 || q.site_ctas < 0)
+    return SITING_EINVAL;
+  for (TunedPlan &t : ctx->tuned)
+    if (t.roi == roi && t.ntests == ntests) {
+      t.plan = q;
+      return SITING_OK;
+    }
+  ctx->tuned.push_back(TunedPlan{roi, ntests, q});
   return SITING_OK;
 }
 

@@ -17,6 +17,16 @@
 // words), which is then written to HBM with coalesced stores.  For windows
 // too large for two CTAs per SM the DEM is read through the read-only L1 path.
 //
+// Half windows: every ray to a target row tx <= ox stays in rows ox-roi..ox,
+// every other ray in rows ox..ox+roi, so an observer can also be swept by two
+// CTAs that each stage roi+1 rows (half the bytes: twice the resident CTAs,
+// and windows up to roi ~150 staged).  The upper CTA writes shed rows 0..roi,
+// the lower one rows roi+1..2roi.  Row ox is the upper CTA's: the lower CTA's
+// rays meet it only in a prefix of steps k with round(k*slope) = 0, and such a
+// prefix samples the cells (ox, oy+-k) in the order and at the steps of the
+// straight ray to (ox, oy+-roi) of the upper CTA, with the same horizons, so
+// its marks there are a subset of that ray's.
+//
 // Bit-exactness: separately rounded FP32 operations, IEEE division for the
 // slopes, round-half-away-from-zero for the minor coordinate.  The horizon
 // slope s = RN(a/k) (a an integer elevation difference, k the step) is
@@ -94,9 +104,18 @@ __device__ __forceinline__ void mark_row_major(const ShedImage &im, int row, int
   atomicOr(&im.R[row * im.rs + (col >> 5)], 1u << (col & 31));
 }
 
-template <bool kRcp, class Dem>
+// Perimeter index of ray t of a half window, in perimeter order: the upper
+// half (0) takes the 4roi+1 targets with tx <= ox, the lower half (1) the
+// other 4roi-1.
+__device__ __forceinline__ int half_ray(int t, int roi, int half) {
+  if (!half) return t + (t <= roi ? 0 : t <= 2 * roi ? roi - 1 : 2 * roi - 1);
+  return t + (t < roi - 1 ? roi + 1 : t < 2 * roi - 1 ? 2 * roi + 1 : 4 * roi + 1);
+}
+
+// Rays of this CTA; the images hold shed rows r0.. (r0 = roi for a lower half).
+template <bool kRcp, bool kHalf, class Dem>
 __device__ __forceinline__ void sweep_rays(const Dem &dem, const ShedArgs &a, int ox, int oy,
-                                           const ShedImage &im, uint32_t rcp) {
+                                           const ShedImage &im, uint32_t rcp, int half) {
   const int roi = a.roi, n = a.n, side = 2 * roi;
   const int roi2 = roi * roi;
   const int xmin = ox - roi, ymin = oy - roi, xmax = ox + roi, ymax = oy + roi;
@@ -104,7 +123,10 @@ __device__ __forceinline__ void sweep_rays(const Dem &dem, const ShedArgs &a, in
   const int obase = dem.base(ox, oy);
   const int oalt = dem.at(obase) + a.oht;
   const float foalt = i2f(oalt), ftht = i2f(a.tht);
-  for (int ip = threadIdx.x; ip < 4 * side; ip += blockDim.x) {
+  const int r0 = kHalf && half ? roi : 0;
+  const int nrays = !kHalf ? 4 * side : half ? 4 * roi - 1 : 4 * roi + 1;
+  for (int t = threadIdx.x; t < nrays; t += blockDim.x) {
+    const int ip = kHalf ? half_ray(t, roi, half) : t;
     int tx, ty;
     if (ip < side) {
       tx = xmin + ip;
@@ -149,7 +171,10 @@ __device__ __forceinline__ void sweep_rays(const Dem &dem, const ShedArgs &a, in
     // the ray's axis, bit pos%32 of word line*stride + pos/32
     const uint32_t img = smem_u32(my ? im.R : im.C);  // shared-memory address
     const int stride = my ? im.rs : im.cs;
-    int pb = obase, pos = roi;
+    // the image line of minor offset 0 and the start's position along the
+    // line, rows counted from r0
+    const int lroi = my ? roi - r0 : roi;
+    int pb = obase, pos = my ? roi : roi - r0;
     const float fend = i2f(kend);
     // elevations and offsets are integers below 2^24: their differences and
     // sums are exact in FP32, so (float)(pelev - oalt) = pelev_f - foalt
@@ -185,7 +210,7 @@ __device__ __forceinline__ void sweep_rays(const Dem &dem, const ShedArgs &a, in
         // pelev + tht against oalt + hs*|i|: both sums in one packed add
         const unsigned long long V = f2_add(f2_pack(fe, foalt), f2_pack(ftht, t));
         if (f2_lo(V) >= f2_hi(V))
-          asm volatile("red.shared.or.b32 [%0], %1;" ::"r"(img + 4u * (uint32_t)((off + roi) * stride + (pos >> 5))),
+          asm volatile("red.shared.or.b32 [%0], %1;" ::"r"(img + 4u * (uint32_t)((off + lroi) * stride + (pos >> 5))),
                        "r"(__funnelshift_l(0u, 1u, pos)) : "memory");  // 1 << (pos & 31)
       }
     } else {
@@ -216,38 +241,43 @@ __device__ __forceinline__ void sweep_rays(const Dem &dem, const ShedArgs &a, in
         }
         const unsigned long long V = f2_add(f2_pack(fe, foalt), f2_pack(ftht, t));
         if (f2_lo(V) >= f2_hi(V))
-          asm volatile("red.shared.or.b32 [%0], %1;" ::"r"(img + 4u * (uint32_t)((off + roi) * stride + (pos >> 5))),
+          asm volatile("red.shared.or.b32 [%0], %1;" ::"r"(img + 4u * (uint32_t)((off + lroi) * stride + (pos >> 5))),
                        "r"(1u << (pos & 31)) : "memory");
       }
     }
   }
 }
 
-// CTAs of at most 800 threads compiled for two resident CTAs per SM (two
-// observers' windows in flight; the per-partition register file then allows
-// 32 registers per thread).
-template <bool kSmem, bool kRcp>
+// One observer (whole window) or one half of one (kHalf: block 2o is the
+// upper half of observer o, block 2o+1 the lower).
+template <bool kSmem, bool kRcp, bool kHalf>
 __device__ __forceinline__ void shed_body(const CUtensorMap &map, const ShedArgs &a) {
   extern __shared__ __align__(128) unsigned char sm[];
   const int nr = 2 * a.roi + 1, nwpr = (nr + 63) / 64, nwords = nr * nwpr;
-  const int ob = a.obs[blockIdx.x];
+  const int half = kHalf ? (int)(blockIdx.x & 1u) : 0;
+  const int obi = kHalf ? (int)(blockIdx.x >> 1) : (int)blockIdx.x;
+  const int r0 = half * a.roi;          // first shed row of this CTA's images
+  const int nri = kHalf ? a.roi + 1 : nr;  // rows of its images and window
+  // the shed rows this CTA writes: the upper half owns row roi
+  const int wr0 = kHalf && half ? a.roi + 1 : 0, wr1 = kHalf && !half ? a.roi + 1 : nr;
+  const int ob = a.obs[obi];
   if (ob < 0 || ob >= a.n * a.n) {  // invalid observer: empty shed, flagged
-    uint64_t *dst = a.sheds + (size_t)blockIdx.x * nwords;
-    for (int i = threadIdx.x; i < nwords; i += blockDim.x) dst[i] = 0ull;
+    uint64_t *dst = a.sheds + (size_t)obi * nwords;
+    for (int i = wr0 * nwpr + threadIdx.x; i < wr1 * nwpr; i += blockDim.x) dst[i] = 0ull;
     if (threadIdx.x == 0) atomicOr(a.err, kErrBadInput);
     return;
   }
   const int ox = ob / a.n, oy = ob - (ob / a.n) * a.n;
-  const int hx0 = ox - a.roi, hy0 = (oy - a.roi) & ~7;  // window origin, 16-byte aligned
+  const int hx0 = ox - a.roi + r0, hy0 = (oy - a.roi) & ~7;  // window origin, 16-byte aligned
   uint16_t *win = reinterpret_cast<uint16_t *>(sm);
   const uint32_t win_bytes = kSmem ? (uint32_t)a.nboxes * a.box_rows * a.win_w * 2u : 0u;
   uint64_t *mbar = reinterpret_cast<uint64_t *>(sm + win_bytes);
   ShedImage im;
   im.rs = shed_row_stride(nr);
-  im.cs = shed_col_stride(nr);
+  im.cs = shed_col_stride(nri);
   im.R = reinterpret_cast<unsigned *>(sm + win_bytes + 16);
-  im.C = im.R + nr * im.rs;
-  const int img_words = nr * im.rs + shed_col_count(nr) * im.cs;
+  im.C = im.R + nri * im.rs;
+  const int img_words = nri * im.rs + shed_col_count(nr) * im.cs;
   float *rcp = reinterpret_cast<float *>(im.R + img_words);  // rcp[k] = RN(1/k)
   if (kRcp)
     for (int i = threadIdx.x; i <= a.roi; i += blockDim.x) rcp[i] = i ? __frcp_rn((float)i) : 0.f;
@@ -260,24 +290,25 @@ __device__ __forceinline__ void shed_body(const CUtensorMap &map, const ShedArgs
   }
   for (int i = threadIdx.x; i < img_words; i += blockDim.x) im.R[i] = 0u;
   __syncthreads();
-  if (threadIdx.x == 0) mark_row_major(im, a.roi, a.roi);  // siting.cpp:279
+  if (threadIdx.x == 0 && !half) mark_row_major(im, a.roi, a.roi);  // siting.cpp:279
   if (kSmem) {
     if (!mbar_wait(mbar, 0)) {
       if (threadIdx.x == 0) atomicOr(a.err, kErrTmaTimeout);
       return;
     }
-    sweep_rays<kRcp>(SmemDem{smem_u32(win), a.win_w, hx0, hy0}, a, ox, oy, im, smem_u32(rcp));
+    sweep_rays<kRcp, kHalf>(SmemDem{smem_u32(win), a.win_w, hx0, hy0}, a, ox, oy, im,
+                            smem_u32(rcp), half);
   } else {
-    sweep_rays<kRcp>(GlobalDem{a.dem, a.pitch}, a, ox, oy, im, smem_u32(rcp));
+    sweep_rays<kRcp, kHalf>(GlobalDem{a.dem, a.pitch}, a, ox, oy, im, smem_u32(rcp), half);
   }
   __syncthreads();
   // fold C into R: one warp per 32x32 block; lane j holds column cb*32+j's
   // bits of rows rb*32..+31, a 5-stage butterfly transpose leaves row rb*32+i
   // in lane i (bit j = column cb*32+j), R's own bit order
-  const int nb32 = (nr + 31) / 32;
+  const int nbr = (nri + 31) / 32, nbc = (nr + 31) / 32;
   const int lane = threadIdx.x & 31;
-  for (int blk = threadIdx.x >> 5; blk < nb32 * nb32; blk += blockDim.x >> 5) {
-    const int rb = blk / nb32, cb = blk - rb * nb32;
+  for (int blk = threadIdx.x >> 5; blk < nbr * nbc; blk += blockDim.x >> 5) {
+    const int rb = blk / nbc, cb = blk - rb * nbc;
     unsigned x = im.C[(cb * 32 + lane) * im.cs + rb];
     if (!__any_sync(0xffffffffu, x != 0u)) continue;
 #pragma unroll
@@ -288,23 +319,33 @@ __device__ __forceinline__ void shed_body(const CUtensorMap &map, const ShedArgs
       x = (lane & sh) ? (x & ~m) | ((o >> sh) & m) : (x & m) | ((o << sh) & ~m);
     }
     const int row = rb * 32 + lane;
-    if (row < nr && x) im.R[row * im.rs + cb] |= x;
+    if (row < nri && x) im.R[row * im.rs + cb] |= x;
   }
   __syncthreads();
-  uint64_t *dst = a.sheds + (size_t)blockIdx.x * nwords;
-  for (int i = threadIdx.x; i < nwords; i += blockDim.x) {
+  uint64_t *dst = a.sheds + (size_t)obi * nwords;
+  for (int i = wr0 * nwpr + threadIdx.x; i < wr1 * nwpr; i += blockDim.x) {
     const int r = i / nwpr, q = i - r * nwpr;
-    const unsigned hi = __brev(im.R[r * im.rs + 2 * q]), lo = __brev(im.R[r * im.rs + 2 * q + 1]);
-    dst[i] = ((uint64_t)hi << 32) | lo;
+    const unsigned *src = im.R + (r - r0) * im.rs + 2 * q;
+    dst[i] = ((uint64_t)__brev(src[0]) << 32) | __brev(src[1]);
   }
 }
 
+// CTAs of at most 800 threads compiled for two resident CTAs per SM (two
+// observers' windows in flight; the per-partition register file then allows
+// 32 registers per thread).
 template <bool kSmem, bool kRcp>
 __global__ void __launch_bounds__(800, 2)
     shed_kernel2(const __grid_constant__ CUtensorMap map, const ShedArgs a) {
-  shed_body<kSmem, kRcp>(map, a);
+  shed_body<kSmem, kRcp, false>(map, a);
 }
 
+// Half windows, staged, one ray a thread: kThreads = 32*ceil((4roi+1)/32),
+// compiled for kMinBlocks resident CTAs per SM (what the window allows).
+template <int kThreads, int kMinBlocks>
+__global__ void __launch_bounds__(kThreads, kMinBlocks)
+    shed_half_kernel(const __grid_constant__ CUtensorMap map, const ShedArgs a) {
+  shed_body<true, true, true>(map, a);
+}
 
 int round8(int v) { return (v + 7) & ~7; }
 
@@ -312,48 +353,73 @@ struct WinGeom {
   int w, box_rows, nboxes;
 };
 
-WinGeom win_geom(int roi) {
+WinGeom win_geom(int roi, bool half) {
   WinGeom g;
-  const int nr = 2 * roi + 1;
+  const int nr = half ? roi + 1 : 2 * roi + 1;  // window rows
   g.w = round8(2 * roi + 8);
   g.nboxes = (nr + 255) / 256;
   g.box_rows = round8((nr + g.nboxes - 1) / g.nboxes);
   return g;
 }
 
+// Half windows are launched for roi 60..151 (4roi+1 rays in at most 608
+// threads).  16384 observers on a 2048^2 DEM, half against whole windows:
+// roi 25 +8%, 50 +0.5%, 75 -1.5%, 100 -8% (staged whole window); 110-120
+// -23..25%, 125-150 -9..13% (whole window through L1).  Below roi 60 the
+// halves' CTAs are too small (a few warps) to gain.
+constexpr int kHalfMinRoi = 60, kHalfMaxRoi = 151;
+
 }  // namespace
 
 size_t shed_smem_bytes(const ShedPlan &p, int roi) {
-  const int nr = 2 * roi + 1;
-  size_t b = 16 + 4 * ((size_t)nr * shed_row_stride(nr) + (size_t)shed_col_count(nr) * shed_col_stride(nr));
+  const int nr = 2 * roi + 1, nri = p.half ? roi + 1 : nr;  // image rows
+  size_t b = 16 + 4 * ((size_t)nri * shed_row_stride(nr) + (size_t)shed_col_count(nr) * shed_col_stride(nri));
   b += 4 * ((size_t)roi + 1);  // reciprocal table
   if (p.use_smem) {
-    const WinGeom g = win_geom(roi);
+    const WinGeom g = win_geom(roi, p.half);
     b += (size_t)g.nboxes * g.box_rows * g.w * 2;
   }
   return b;
 }
 
-ShedPlan shed_default_plan(int roi) {
-  // one ray per thread up to 800 rays (two resident CTAs per SM at 32
-  // registers a thread), else an even split into rounds of at most 800: a
-  // single 1024-thread CTA per SM ran 1.5x slower per ray step (roi 104-128)
+namespace {
+
+// One CTA an observer: one ray per thread up to 800 rays (two resident CTAs
+// per SM at 32 registers a thread), else an even split into rounds of at most
+// 800 (a single 1024-thread CTA per SM ran 1.5x slower per ray step, roi
+// 104-128).  The window is staged only while two CTAs of a full round of rays
+// still share an SM: a ray's steps form one dependent chain, so fewer
+// resident warps cannot hide the shared-memory latency and the L1 path, with
+// more resident CTAs, is faster.
+ShedPlan shed_whole_plan(int roi) {
   const int rays = 8 * roi;
   const int rounds = (rays + 799) / 800;
   const int threads = std::min(800, ((rays + rounds - 1) / rounds + 31) / 32 * 32);
-  ShedPlan p{std::max(threads, 64), true};
-  // the window is staged only while two CTAs of a full round of rays still
-  // share an SM: a ray's steps form one dependent chain, so fewer resident
-  // warps cannot hide the shared-memory latency and the L1 path, with more
-  // resident CTAs, is faster (roi > 100 split into rounds: L1)
+  ShedPlan p{std::max(threads, 64), true, false};
   if (rounds > 1 || shed_smem_bytes(p, roi) > 112 * 1024) p.use_smem = false;
   return p;
 }
 
+// Two CTAs an observer, each staging its half window, one ray a thread.
+ShedPlan shed_half_plan(int roi) { return ShedPlan{(4 * roi + 1 + 31) / 32 * 32, true, true}; }
+
+}  // namespace
+
+ShedPlan shed_default_plan(int roi) {
+  return roi >= kHalfMinRoi && roi <= kHalfMaxRoi ? shed_half_plan(roi) : shed_whole_plan(roi);
+}
+
+// smem: 1 half windows (up to roi 151, else as 2), 2 the whole window,
+// staged where it fits, 0 the whole window through L1, -1 the default.
 ShedPlan shed_plan_for(int roi, int smem) {
-  ShedPlan p = shed_default_plan(roi);
-  if (smem == 0) p.use_smem = false;
-  return p;  // the window is staged only where the default allows it
+  if (smem == 1 && roi >= 1 && roi <= kHalfMaxRoi) return shed_half_plan(roi);
+  if (smem == 1 || smem == 2) return shed_whole_plan(roi);
+  if (smem == 0) {
+    ShedPlan p = shed_whole_plan(roi);
+    p.use_smem = false;
+    return p;
+  }
+  return shed_default_plan(roi);
 }
 
 cudaError_t launch_sheds(const DemView &dem, int roi, int oht, int tht, int nsheds,
@@ -371,30 +437,40 @@ cudaError_t launch_sheds(const DemView &dem, int roi, int oht, int tht, int nshe
   a.obs = obs;
   a.sheds = sheds;
   a.err = d_err;
+  // the reciprocal-table division is exhaustively checked for |a| <= 2^21
+  // (heights up to 10^6 over 16-bit elevations) and steps up to 2048
+  const bool rcp = roi <= 2048 && oht >= 0 && oht <= 1000000;
+  // half windows need the staged window and the table division
+  ShedPlan eff = plan;
+  if (eff.half && (!rcp || !dem.tma_ok || roi < 1 || roi > kHalfMaxRoi)) eff = shed_whole_plan(roi);
+  eff.use_smem = eff.use_smem && dem.tma_ok;
   CUtensorMap map;
   memset(&map, 0, sizeof(map));
-  const bool smem = plan.use_smem && dem.tma_ok;
-  if (smem) {
-    const WinGeom g = win_geom(roi);
+  if (eff.use_smem) {
+    const WinGeom g = win_geom(roi, eff.half);
     a.win_w = g.w;
     a.box_rows = g.box_rows;
     a.nboxes = g.nboxes;
     if (!make_dem_tensor_map(&map, dem, g.w, g.box_rows)) return cudaErrorInvalidValue;
   }
-  ShedPlan eff = plan;
-  eff.use_smem = smem;
   const size_t shm = shed_smem_bytes(eff, roi);
-  auto launch = [&](auto kern) -> cudaError_t {
+  auto launch = [&](auto kern, int ctas) -> cudaError_t {
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shm);
     if (e != cudaSuccess) return e;
-    kern<<<nsheds, plan.threads, shm, st>>>(map, a);
+    kern<<<ctas, eff.threads, shm, st>>>(map, a);
     return cudaSuccess;
   };
-  // the reciprocal-table division is exhaustively checked for |a| <= 2^21
-  // (heights up to 10^6 over 16-bit elevations) and steps up to 2048
-  const bool rcp = roi <= 2048 && oht >= 0 && oht <= 1000000;
-  const cudaError_t e = smem ? (rcp ? launch(shed_kernel2<true, true>) : launch(shed_kernel2<true, false>))
-                             : (rcp ? launch(shed_kernel2<false, true>) : launch(shed_kernel2<false, false>));
+  cudaError_t e;
+  if (eff.half) {
+    // the variant compiled for as many resident CTAs as the window allows
+    e = eff.threads <= 416   ? launch(shed_half_kernel<416, 4>, 2 * nsheds)
+        : eff.threads <= 512 ? launch(shed_half_kernel<512, 3>, 2 * nsheds)
+                             : launch(shed_half_kernel<608, 2>, 2 * nsheds);
+  } else if (eff.use_smem) {
+    e = rcp ? launch(shed_kernel2<true, true>, nsheds) : launch(shed_kernel2<true, false>, nsheds);
+  } else {
+    e = rcp ? launch(shed_kernel2<false, true>, nsheds) : launch(shed_kernel2<false, false>, nsheds);
+  }
   if (e != cudaSuccess) return e;
   return cudaGetLastError();
 }

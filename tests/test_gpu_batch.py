@@ -44,6 +44,7 @@ def test_batch_matches_oracle(ctx, oracle, native):
     dict(vix_tile=16, vix_smem=1, shed_smem=1, site_ctas=1),
     dict(vix_tile=64, vix_smem=0, shed_smem=0, site_ctas=3),
     dict(vix_tile=32, vix_smem=1, shed_smem=-1, site_ctas=16),
+    dict(vix_tile=16, vix_smem=1, shed_smem=2, site_ctas=2),
 ])
 def test_batch_plans_do_not_change_results(ctx, oracle, native, plan):
     jobs = _mixed_jobs(native, 5, 2)

@@ -131,17 +131,41 @@ def test_unaligned_and_tiny_dems_dev(ctx, oracle, native, n):
     _diff("vix", d_vix.cpu().numpy(), want)
 
 
-@pytest.mark.parametrize("roi", [1, 2, 63, 64, 130, 200])
+@pytest.mark.parametrize("roi", [1, 2, 3, 59, 60, 64, 100, 104, 127, 130, 151, 152, 200])
 def test_viewshed_roi_range(ctx, oracle, native, roi):
-    """Window staged by TMA (roi <= 124) and read through L1 (larger roi)."""
+    """Default plans: whole windows staged (roi < 60), half windows staged
+    (roi 60..151, three launch shapes), whole windows through L1 (larger)."""
     n = 300
     dem = native.fbm_dem(n, roi, octaves=7, range_max=9000)
     rng = np.random.default_rng(roi)
     obs = np.sort(rng.choice(n * n, 40, replace=False)).astype(np.int32)
     obs[:4] = [0, n - 1, n * n - 1, n * (n - 1)]  # corners
+    obs[4:8] = [n // 2, n * (n // 2), n * (n // 2) + n - 1, n * (n - 1) + n // 2]  # edge midpoints
     want = oracle.sheds(dem, n, roi, 30, 30, obs)
     got = ctx.calc_sheds(n, dem, roi, 30, 30, obs)
     _diff("sheds", got, want)
+
+
+@pytest.mark.parametrize("roi", [1, 5, 50, 100, 120])
+def test_viewshed_window_forms_agree(ctx, oracle, native, roi):
+    """Half windows, the whole window staged and the whole window through L1
+    (plans 1, 2 and 0) give the oracle's sheds, on a flat-topped DEM whose
+    ties and horizontal sight lines stress the row shared by the halves."""
+    n = 260
+    dem = native.fbm_dem(n, 7 * roi, octaves=6, range_max=3000)
+    dem.reshape(n, n)[100:160, 90:170] = 1500  # a plateau: equal elevations along straight rays
+    rng = np.random.default_rng(roi + 1)
+    obs = np.sort(rng.choice(n * n, 24, replace=False)).astype(np.int32)
+    obs[:3] = [130 * n + 130, 100 * n + 90, 159 * n + 169]
+    obs.sort()
+    want = oracle.sheds(dem, n, roi, 12, 12, obs)
+    for smem in (1, 2, 0):
+        ctx.autotune_clear()
+        ctx.autotune_set(roi, 1, native.Plan(shed_smem=smem))
+        _diff(f"sheds (plan {smem})", ctx.calc_sheds(n, dem, roi, 12, 12, obs), want)
+    ctx.autotune_clear()
+    with pytest.raises(native.SitingError):
+        ctx.autotune_set(roi, 1, native.Plan(shed_smem=3))
 
 
 @pytest.mark.parametrize("roi,ntests", [(1, 1), (3, 1000), (124, 40), (160, 33)])

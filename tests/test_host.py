@@ -180,3 +180,12 @@ def test_batch_knobs_reject_a_missing_context(native):
     assert lib.siting_ctx_set_batch_mode(None, 1) == native.EINVAL
     assert lib.siting_ctx_set_batch_graphs(None, 1) == native.EINVAL
     assert lib.siting_ctx_batch_graph_stats(None, C.byref(c), C.byref(r)) == native.EINVAL
+
+
+def test_autotune_set_checks_its_arguments(native):
+    """A pinned plan needs a context and fields in range (no device work)."""
+    import ctypes as C
+
+    lib = native.load()
+    pc = native.Plan(shed_smem=2).c()
+    assert lib.siting_autotune_set(None, 100, 16, C.byref(pc)) == native.EINVAL
