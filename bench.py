@@ -313,12 +313,13 @@ NCU_TRAFFIC = {
 }
 
 # Warp instructions per unit of work of the two issue-bound stages, from ncu
-# (smsp__inst_executed.sum of one launch / its units) on the 2048^2 capture
-# with roi 100 and 100 targets: per target for VIX, per observer for
-# VIEWSHED.  Keyed by the parameters they were measured with.
+# (smsp__inst_executed.sum of one launch / its units) on the 2048^2 captures
+# with roi 100 and 100 targets: per target for VIX (vix_kernel), per observer
+# for VIEWSHED (shed_half_kernel, both halves).  Keyed by the parameters they
+# were measured with.
 ISSUE_WORK = {
     ("vix", 100, 100): (2.058e9 / (2048 * 2048 * 100), "target"),
-    ("viewshed", 100, 100): (1.354e9 / 16384, "observer"),
+    ("viewshed", 100, 100): (1.398323148e9 / 16384, "observer"),
 }
 ISSUE_SLOTS_PER_SM = 4  # one warp instruction per cycle from each SM sub-partition
 
