@@ -306,9 +306,9 @@ def stage_bytes(w, nwanted, site_bytes):
 
 
 # DRAM bytes per launch (dram__bytes_read.sum + dram__bytes_write.sum) from
-# ncu: VIX, VIEWSHED and SITE captured at full size (4096^2 launch list).
+# ncu: VIX, VIEWSHED (shed_half_kernel) and SITE captured at full size.
 NCU_TRAFFIC = {
-    "c2_4096": {"vix": 33720064 + 1536, "viewshed": 34480896 + 365585152,
+    "c2_4096": {"vix": 33720064 + 1536, "viewshed": 33861632 + 361607680,
                 "site": 2494835712 + 10062080},
 }
 
