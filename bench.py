@@ -206,9 +206,13 @@ def run_gpu(args, w):
     ctx = sg.Context(local)
     if args.site_ctas:
         ctx.set_site_ctas(args.site_ctas)
-    tuned = None
+    plan_desc = "library default"
     if args.autotune:  # one-off, before the clock: plans timed on a corner of the DEM
-        tuned = ctx.autotune(p, dem, sample_rows=args.autotune_rows)
+        plan_desc = "autotuned " + str(ctx.autotune(p, dem, sample_rows=args.autotune_rows))
+    if args.shed_plan is not None:  # a VIEWSHED window form pinned for this job's roi
+        pinned = sg.Plan(shed_smem=args.shed_plan)
+        ctx.autotune_set(w["roi"], w["ntests"], pinned)
+        plan_desc = "pinned " + str(pinned)
     stream = torch.cuda.ExternalStream(ctx.stream)
 
     # device-resident buffers
@@ -273,7 +277,7 @@ def run_gpu(args, w):
         "ms_per_step": mean_dev, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32/u64", "data": "synthetic",
         "config": workload_config(args, w, world, g.nwanted),
-        "plan": "autotuned " + str(tuned) if tuned else "library default",
+        "plan": plan_desc,
         "e2e": {"value": world * n * n / (mean_e2e / 1e3), "unit": "cells/s",
                 "ms_per_step": mean_e2e, "h2d_bytes_per_step": n * n * 2,
                 "d2h_bytes_per_step": g.nwanted * 5},
@@ -944,6 +948,9 @@ def main():
     ap.add_argument("--autotune", action="store_true",
                     help="time the launch plans on a corner of the DEM first (siting_autotune)")
     ap.add_argument("--autotune-rows", type=int, default=1024)
+    ap.add_argument("--shed-plan", type=int, default=None, choices=[0, 1, 2],
+                    help="VIEWSHED window form (siting_autotune_set): 1 half windows, "
+                         "2 the whole window, 0 the whole window through L1")
     ap.add_argument("--serve-requests", type=int, default=2000)
     ap.add_argument("--serve-rate", type=float, default=100.0, help="mean arrivals per second")
     ap.add_argument("--serve-budget-gb", type=float, default=150.0)
